@@ -1,0 +1,435 @@
+"""Benchmark: batched forward+adjoint gradients of the inv.cu hot path on GB300.
+
+Workload (the configuration the headline metric is quoted on): SH on a
+681 x 141 grid at 12.5 m, dt = 1 ms, 4000 steps, 12 layers with vs from 1200
+to 3500 m/s, 3 dipping normal faults with seeded throws, Gardner density,
+16 shots at f0 = 8 Hz, 681 surface receivers, envelope misfit, Gaussian
+smoothing sigma = 5 cells, forward checkpoints every 10 steps. One bench step
+is one gradient (Misfit::run(kernel=true)): all 16 forward solves, the
+envelope misfit and adjoint sources, all 16 adjoint solves with kernel
+accumulation, and the smoothing of the three kernels.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`value` is shots/s (forward+adjoint pairs) with inputs resident in HBM,
+timed with CUDA events on the solver's stream; `e2e` is the same metric
+through the C ABI from pinned host buffers (model and observed traces in,
+kernels and misfit out, copies inside the timed region). The reference arm
+times the CPU port of the reference algorithm (oracle/, OpenMP on all host
+cores) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "shots/s fwd+adj & cell-updates/s (% HBM peak) vs plain path; p50/p99 solve latency"
+
+# ----------------------------------------------------------------------------
+# Workload
+# ----------------------------------------------------------------------------
+NX, NZ, H, DT, NT, NSHOT, F0, SFE, SIGMA = 681, 141, 12.5, 1e-3, 4000, 16, 8.0, 10, 5
+SEED = 2024
+
+
+def faulted_model(nx=NX, nz=NZ, h=H, seed=SEED, nlayer=12, vs_top=1200.0, vs_bottom=3500.0, nfault=3):
+    """vs, vp, rho (float32, reference layout) of a layered model cut by
+    dipping normal faults with seeded throws; vp = 1.73 vs, rho Gardner."""
+    rng = np.random.default_rng(seed)
+    x = (np.arange(nx) * h)[:, None]
+    z = (np.arange(nz) * h)[None, :]
+    zmax = (nz - 1) * h
+    shift = np.zeros((nx, nz))
+    for f in range(nfault):
+        x0 = (0.2 + 0.6 * (f + rng.uniform(0.2, 0.8)) / nfault) * (nx - 1) * h
+        dip = math.radians(rng.uniform(50, 70))
+        throw = rng.uniform(0.03, 0.08) * zmax
+        shift += np.where(x > x0 + z / math.tan(dip), throw, 0.0)
+    thick = zmax / nlayer
+    layer = np.clip(np.floor((z - shift) / thick), 0, nlayer - 1).astype(int)
+    vs = np.linspace(vs_top, vs_bottom, nlayer)[layer]
+    vp = 1.73 * vs
+    rho = 310.0 * vp ** 0.25
+    f32 = lambda a: np.ascontiguousarray(a.astype(np.float32).ravel())
+    return f32(vs), f32(vp), f32(rho)
+
+
+def smooth(a, nx, nz, cells):
+    """Separable Gaussian blur (initial model), plain numpy."""
+    a = a.reshape(nx, nz).astype(np.float64)
+    r = int(3 * cells)
+    w = np.exp(-0.5 * (np.arange(-r, r + 1) / cells) ** 2)
+    w /= w.sum()
+    pad = np.pad(a, r, mode="edge")
+    t = sum(w[q] * pad[q:q + nx, :] for q in range(2 * r + 1))
+    t = sum(w[q] * t[:, q:q + nz] for q in range(2 * r + 1))
+    return np.ascontiguousarray(t.astype(np.float32).ravel())
+
+
+def lame(vs, vp, rho):
+    f32 = np.float32
+    lam = np.where(vp > vs, (rho * (vp * vp - f32(2) * vs * vs)).astype(f32), f32(0)).astype(f32)
+    mu = (rho * vs * vs).astype(f32)
+    return lam, mu, rho
+
+
+def workload():
+    xmax, zmax = (NX - 1) * H, (NZ - 1) * H
+    src = [[xmax * (s + 0.5) / NSHOT, 2 * H, 0, F0, 1.2 / F0, 0.0, 1e10] for s in range(NSHOT)]
+    rec = [[i * H, 0.0] for i in range(NX)]
+    values = {"mode": 2, "sh": 1, "psv": 0, "nt": NT, "dt": DT, "sfe": SFE, "model_type": 0, "trace_type": 0,
+              "abs_left": 1, "abs_right": 1, "abs_bottom": 1, "abs_top": 0, "abs_width": 20, "abs_alpha": 0.015,
+              "inv_lambda": 0, "inv_mu": 1, "inv_rho": 1, "misfit": 1, "filter": 0, "filter_sigma": SIGMA}
+    vs, vp, rho = faulted_model()
+    init = [smooth(a, NX, NZ, 250.0 / H / 2) for a in (vs, vp, rho)]
+    return dict(xmax=xmax, zmax=zmax, src=src, rec=rec, values=values, true=lame(vs, vp, rho),
+                init=lame(*init))
+
+
+CONFIG_DESC = {
+    "workload": "SH gradient, 681x141 grid at 12.5 m, dt 1 ms, 4000 steps, 16 shots f0 8 Hz, 681 receivers, "
+                "envelope misfit, Gaussian smoothing sigma 5, checkpoints every 10 steps",
+    "grid": [NX, NZ], "nt": NT, "shots": NSHOT, "receivers": NX, "sfe": SFE, "misfit": "envelope",
+    "filter_sigma": SIGMA, "step": "one gradient: 16 forward + envelope misfit + 16 adjoint + smoothing",
+    "l2": "flushed (256 MB write) between timed steps; each step also streams 3.1 GB of checkpoints",
+}
+
+
+# ----------------------------------------------------------------------------
+# Helpers
+# ----------------------------------------------------------------------------
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """Samples nvidia-smi every 200 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.out = tempfile.NamedTemporaryFile(mode="w+", suffix=".csv", delete=False)
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.out, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        self.out.flush()
+        self.out.seek(0)
+        rows = [r.split(",") for r in self.out.read().strip().splitlines() if r.strip()]
+        os.unlink(self.out.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in rows if len(r) > 2 and r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) > 2 and r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            for q, nm in enumerate(names):
+                if len(r) > 5 + q and r[5 + q].strip().lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(kernel_tag):
+    """DRAM bytes per launch of the step kernel from the committed ncu
+    summary (profiles/dram_traffic.txt: `<tag> <bytes per launch> <note>`)."""
+    p = os.path.join(ROOT, "profiles", "dram_traffic.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        parts = line.split()
+        if len(parts) >= 2 and parts[0] == kernel_tag and not line.startswith("#"):
+            try:
+                return float(parts[1])
+            except ValueError:
+                return None
+    return None
+
+
+# ----------------------------------------------------------------------------
+# CPU port of the reference (oracle), bounded sample
+# ----------------------------------------------------------------------------
+def cpu_sample(wl, nshots=1):
+    """Times the oracle (C restatement of the reference, OpenMP over all host
+    cores) on `nshots` full shots of the workload: forward with checkpoints,
+    envelope misfit, adjoint; plus one smoothing of the three kernels.
+    Returns (seconds per 16-shot gradient, threads, description)."""
+    from oracle import oracle as orc
+
+    orc.set_threads(os.cpu_count() or 1)
+    threads = orc.num_threads()
+    lam, mu, rho = wl["init"]
+    v = wl["values"]
+    nt = NT
+    src = np.array(wl["src"], np.float32)
+    rec = np.array(wl["rec"], np.float32)
+    stf = [np.zeros(len(src) * nt, np.float32) for _ in range(3)]
+    for s in range(len(src)):
+        c = orc.ricker(nt, DT, *src[s, 3:7])
+        for q in range(3):
+            stf[q][s * nt:(s + 1) * nt] = c[q]
+    ab = orc.absbound(NX, NZ, v["abs_width"], v["abs_alpha"], 1, 1, 1, 0)
+    dx = float(np.float32(wl["xmax"]) / np.float32(NX - 1))
+    pb = orc.Problem(nx=NX, nz=NZ, nt=nt, dx=dx, dz=dx, dt=DT, sh=True, psv=False, sfe=SFE, lam=lam, mu=mu,
+                     rho=rho, ab=ab, stf=tuple(stf),
+                     src_id=(orc.calc_idx(src[:, 0], wl["xmax"], NX), orc.calc_idx(src[:, 1], wl["zmax"], NZ)),
+                     rec_id=(orc.calc_idx(rec[:, 0], wl["xmax"], NX), orc.calc_idx(rec[:, 1], wl["zmax"], NZ)),
+                     inv_lambda=False, inv_mu=True, inv_rho=True)
+    t0 = time.perf_counter()
+    kern = None
+    for s in range(nshots):
+        _, oy, _, ck = orc.forward(pb, s, adj=True)
+        _, ad = orc.envelope_misfit(oy, oy * np.float32(0.9), DT)
+        kern = orc.adjoint(pb, [np.zeros_like(ad), ad, np.zeros_like(ad)], ck, kern)
+    t_shot = (time.perf_counter() - t0) / nshots
+    t1 = time.perf_counter()
+    for k in kern:
+        orc.gaussian_filter(NX, NZ, SIGMA, k)
+    t_filter = time.perf_counter() - t1
+    desc = ("%d of %d shots at full size (forward %d steps with checkpoints, envelope misfit, adjoint) plus "
+            "one smoothing of 3 kernels; per-gradient time = 16 x shot + smoothing" % (nshots, NSHOT, nt))
+    return NSHOT * t_shot + t_filter, threads, desc
+
+
+# ----------------------------------------------------------------------------
+# GPU arm
+# ----------------------------------------------------------------------------
+def run_ours(args, ws, rank, local):
+    import __graft_entry__ as ge
+
+    pkg = ge.load_package()
+    if pkg.device_count() < 1:
+        raise RuntimeError("no CUDA device")
+    pkg.select_device(local)
+    wl = workload()
+    tmp = tempfile.mkdtemp(prefix="gbfwi_bench_")
+    cfg = pkg.Config.new(tmp, wl["values"], wl["src"], wl["rec"])
+    sol = pkg.FdmSolver(cfg, grid=(NX, NZ, wl["xmax"], wl["zmax"]))
+    sol.set_option("batch", NSHOT)
+    # observed data on the true model (setup, not timed)
+    sol.set_model_grid(*wl["true"])
+    sol.run_forward_batch(list(range(NSHOT)))
+    obs = np.stack([sol.out("y", slot=b) for b in range(NSHOT)])
+    sol.set_model_grid(*wl["init"])
+    filt = pkg.GaussianFilter(NX, NZ, SIGMA)
+    mis = pkg.Misfit.from_obs(1, sol, {"y": obs}, filt)
+    flush = pkg.DeviceArray(np.zeros(64 << 20, np.float32))  # 256 MB
+    zeros = np.zeros(64 << 20, np.float32)
+
+    def l2_flush():
+        pkg.h2d(flush.ptr, zeros)
+
+    for _ in range(args.warmup):
+        mis.run(kernel=True)
+    sol.stats(reset=True)
+    step_ms = []
+    barrier(ws)
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            l2_flush()
+            pkg.lib().gb_device_sync()
+            sol.timer_begin()
+            mis.run(kernel=True)
+            step_ms.append(sol.timer_end())
+    st = sol.stats()
+    barrier(ws)
+    total_ms = max_over_ranks(sum(step_ms), ws)
+    value = NSHOT * args.steps * ws / (total_ms / 1e3)
+    cells = NX * NZ
+
+    # roofline of the fused step kernel (SH: 40 algorithmic bytes per cell-update)
+    per_launch_ms = st.step_ms / max(st.step_launches, 1)
+    algo_bytes = 40.0 * cells * NSHOT
+    achieved = algo_bytes / (per_launch_ms * 1e-3) / 1e9
+    peak, peak_kind = peaks()
+    roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 3), "traffic": profiled_traffic("step_sh_c2"),
+            "kernel": "k_step<SH> (fused velocity+stress step, 16 shots per launch)",
+            "algorithmic_bytes_per_launch": algo_bytes, "avg_launch_us": round(per_launch_ms * 1e3, 2),
+            "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+            "note": "state (16 shots x 4 fields + model) is L2-resident at this size; see profiles/"}
+
+    # end to end through the C ABI with pinned host buffers
+    n_obs = obs.size
+    h_obs = pkg.PinnedArray(n_obs)
+    h_obs.array[:] = obs.ravel()
+    h_model = [pkg.PinnedArray(cells) for _ in range(3)]
+    for q in range(3):
+        h_model[q].array[:] = wl["init"][q]
+    h_k = [pkg.PinnedArray(cells) for _ in range(2)]
+    e2e_ms = []
+    mis_val = None
+    for _ in range(args.steps):
+        l2_flush()
+        pkg.lib().gb_device_sync()
+        t0 = time.perf_counter()
+        pkg.check(pkg.lib().gb_set_model_grid(sol._h, *[pkg._ptr(m.array) for m in h_model]))
+        pkg.check(pkg.lib().gb_misfit_set_obs(mis._h, None, pkg._ptr(h_obs.array), None))
+        mis_val = mis.run(kernel=True)
+        for q, which in enumerate((pkg.GB_K_MU, pkg.GB_K_RHO)):
+            pkg.check(pkg.lib().gb_memcpy_d2h(h_k[q].ptr, sol.ptr(which), cells * 4))
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e_total = max_over_ranks(sum(e2e_ms), ws)
+    e2e = {"value": round(NSHOT * args.steps * ws / (e2e_total / 1e3), 3), "unit": "shots/s",
+           "h2d_bytes_per_step": int(3 * cells * 4 + n_obs * 4), "d2h_bytes_per_step": int(2 * cells * 4 + 8),
+           "ms_per_step": round(e2e_total / args.steps, 3)}
+
+    # plain path: one shot per launch sequence, no graphs (same GPU, one gradient)
+    plain = None
+    if rank == 0 and not args.no_plain:
+        cfgp = pkg.Config.new(tmp, dict(wl["values"], batch=1, graphs=0), wl["src"], wl["rec"])
+        sp = pkg.FdmSolver(cfgp, grid=(NX, NZ, wl["xmax"], wl["zmax"]))
+        sp.set_option("batch", 1)
+        sp.set_option("graphs", 0)
+        sp.set_model_grid(*wl["init"])
+        mp = pkg.Misfit.from_obs(1, sp, {"y": obs}, pkg.GaussianFilter(NX, NZ, SIGMA))
+        mp.run(kernel=True)
+        sp.timer_begin()
+        mp.run(kernel=True)
+        plain_ms = sp.timer_end()
+        plain = {"value": round(NSHOT / (plain_ms / 1e3), 3), "unit": "shots/s", "ms_per_step": round(plain_ms, 2),
+                 "what": "batch 1, no CUDA graphs, same kernels"}
+        mp.close()
+        sp.close()
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        t_grad, threads, desc = cpu_sample(wl)
+        cpu = {"value": round(NSHOT / t_grad, 4), "unit": "shots/s", "cores": threads, "kind": "port",
+               "sample": desc}
+    clocks = clk.summary()
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "shots/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded faulted layered model with the workload's shapes; no dataset)",
+        "config": dict(CONFIG_DESC, batch=st.batch_capacity, tile=[st.tile_tz, st.tile_tx],
+                       ckpt="fp32", parallelism="shots sharded over %d rank(s), replicas" % ws),
+        "cell_updates_per_s": round(2.0 * cells * NT * NSHOT * args.steps * ws / (total_ms / 1e3), 1),
+        "misfit": mis_val, "plain_path": plain, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+        "gpu_launches": int(st.launches), "clocks": clocks,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    wl = workload()
+    samples = []
+    threads, desc = 0, ""
+    for q in range(args.warmup + args.steps):
+        t_grad, threads, desc = cpu_sample(wl)
+        if q >= args.warmup:
+            samples.append(t_grad)
+    value = NSHOT / (sum(samples) / len(samples))
+    line = {
+        "metric": METRIC, "value": round(value, 4), "unit": "shots/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(1e3 * sum(samples) / len(samples), 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded faulted layered model with the workload's shapes; no dataset)",
+        "config": dict(CONFIG_DESC, parallelism="host cores"), "impl": "reference",
+        "cpu_baseline": {"value": round(value, 4), "unit": "shots/s", "cores": threads, "kind": "port",
+                         "sample": desc},
+        "e2e": {"value": round(value, 4), "unit": "shots/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference's path is CUDA only; its CPU restatement (oracle/, pinned against the "
+                "reference's golden seismograms) is the CPU implementation timed here",
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------
+_PG = None
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(v, ws):
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain-path leg")
+    args = ap.parse_args()
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    try:
+        if args.impl == "reference":
+            run_reference(args, ws, rank)
+        else:
+            run_ours(args, ws, rank, local)
+    finally:
+        if ws > 1:
+            import torch.distributed as dist
+
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

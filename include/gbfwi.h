@@ -1,0 +1,228 @@
+/*
+ * gbfwi — GB300-native drop-in for the hot path of libccy/inv.cu.
+ *
+ * C ABI of libgbfwi.so: plain pointers, sizes and opaque handles. Every call
+ * returns a status (GB_OK == 0) unless it returns a handle or pointer (NULL on
+ * error); gb_last_error() describes the last failure on the calling thread.
+ * Calls are synchronous, like the reference's default-stream code: when a
+ * call returns, its device results are visible to the next call and to any
+ * other CUDA user of the device.
+ *
+ * Device buffers returned by gb_solver_ptr() use the reference layout
+ * float[nx*nz] with k = i*nz + j (z contiguous) for grids, and
+ * float[nrec*nt] with k = ir*nt + it for traces. They stay valid for the
+ * solver's lifetime and may be updated in place between calls (the
+ * reference's optimizer aliases lambda/mu/rho and k_* this way).
+ *
+ * Each declaration names the reference interface it replaces.
+ */
+#ifndef GBFWI_H
+#define GBFWI_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GB_VERSION 1
+
+/* status codes */
+#define GB_OK 0
+#define GB_ERR_ARG 1    /* invalid argument or size */
+#define GB_ERR_CUDA 2   /* CUDA runtime or launch failure */
+#define GB_ERR_IO 3     /* file missing or malformed */
+#define GB_ERR_BUDGET 4 /* request does not fit the HBM budget */
+#define GB_ERR_STATE 5  /* call not valid in the current state */
+#define GB_ERR_MODEL 6  /* model size does not match the grid */
+
+/* gb_solver_ptr() selectors */
+enum gb_buffer {
+    GB_OUT_X = 0, GB_OUT_Y, GB_OUT_Z,
+    GB_ADSTF_X, GB_ADSTF_Y, GB_ADSTF_Z,
+    GB_LAMBDA, GB_MU, GB_RHO,
+    GB_K_LAMBDA, GB_K_MU, GB_K_RHO,
+    GB_STF_X, GB_STF_Y, GB_STF_Z
+};
+
+/* Last error message of the calling thread (never NULL). */
+const char *gb_last_error(void);
+/* ABI version (GB_VERSION). */
+int gb_version(void);
+
+/* ------------------------------------------------------------------ Config
+ * Replaces class Config (lib/config.h:86-108) and the argument handling of
+ * main (inv.cu:12-30). */
+typedef struct gb_config gb_config;
+
+/* Config(map&) (lib/config.h:92-108): overrides are "-key=value" or
+ * "key=value" strings that win over config.ini; reads sources.dat and
+ * stations.dat; honours `clean` and creates dir/output. */
+gb_config *gb_config_load(const char *dir, int noverrides, const char *const *overrides);
+/* Empty configuration rooted at dir (for callers without files). */
+gb_config *gb_config_new(const char *dir);
+void gb_config_free(gb_config *cfg);
+/* Sets one key as if read from config.ini with the highest priority. */
+int gb_config_set(gb_config *cfg, const char *key, const char *value);
+/* config->f / config->i lookups; missing keys read as 0. */
+int gb_config_has(const gb_config *cfg, const char *key);
+float gb_config_f(const gb_config *cfg, const char *key);
+int gb_config_i(const gb_config *cfg, const char *key);
+const char *gb_config_path(const gb_config *cfg);
+/* config->src (7 floats: x z type f0 t0 angle amp) and config->rec (x z). */
+int gb_config_nsrc(const gb_config *cfg);
+int gb_config_nrec(const gb_config *cfg);
+int gb_config_source(const gb_config *cfg, int is, float out[7]);
+int gb_config_station(const gb_config *cfg, int ir, float out[2]);
+int gb_config_add_source(gb_config *cfg, const float src[7]);
+int gb_config_add_station(gb_config *cfg, const float rec[2]);
+
+/* ------------------------------------------------------------------ Solver
+ * Replaces class Solver (solver/solver.h:7-268) and FdmSolver
+ * (solver/fdm.h:222-613), selected by solver = 0 (lib/index.h:33-38). */
+typedef struct gb_solver gb_solver;
+
+/* Solver::init + FdmSolver::init (solver/solver.h:158-224,
+ * solver/fdm.h:350-462): grid inferred from model_true/proc000000_{x,z}.bin. */
+gb_solver *gb_solver_create(const gb_config *cfg);
+/* Same, with the grid given instead of read from model files:
+ * dx = xmax/(nx-1), dz = zmax/(nz-1). */
+gb_solver *gb_solver_create_grid(const gb_config *cfg, int nx, int nz, float xmax, float zmax);
+void gb_solver_destroy(gb_solver *s);
+
+/* Solver::importModel + FdmSolver::importModel (solver/solver.h:225-252,
+ * solver/fdm.h:463-476): reads model_true (model_true != 0) or model_init,
+ * maps the points onto the grid (mesh2grid, nearest point, first wins) and
+ * converts vp/vs to lambda/mu when model_type == 0. */
+int gb_import_model(gb_solver *s, int model_true);
+/* The same from host arrays of npt model points (x, z, vp|lambda, vs|mu, rho). */
+int gb_set_model_points(gb_solver *s, int npt, const float *x, const float *z, const float *a, const float *b,
+                        const float *rho);
+/* Host lambda, mu, rho already on the grid (reference layout). */
+int gb_set_model_grid(gb_solver *s, const float *lambda, const float *mu, const float *rho);
+
+/* FdmSolver::runForward (solver/fdm.h:515-570). isrc < 0 fires every source
+ * at once. trace != 0 writes output/{v|u}{x,y,z}_NNNNNN.su; snapshot != 0
+ * writes wavefield snapshots every wfe steps. */
+int gb_run_forward(gb_solver *s, int isrc, int trace, int snapshot);
+/* FdmSolver::runAdjoint (solver/fdm.h:571-612): adjoint sources from
+ * GB_ADSTF_*, kernels accumulated into GB_K_*. snapshot uses wae. */
+int gb_run_adjoint(gb_solver *s, int isrc, int snapshot);
+/* FdmSolver::initKernels (solver/fdm.h:495-499). */
+int gb_init_kernels(gb_solver *s);
+/* FdmSolver::exportAxis (solver/fdm.h:500-514). */
+int gb_export_axis(gb_solver *s);
+/* FdmSolver::exportModel (solver/fdm.h:477-494). */
+int gb_export_model(gb_solver *s, int n);
+/* Solver::exportKernel (solver/solver.h:255-259). */
+int gb_export_kernel(gb_solver *s, int n);
+/* Solver::exportTraces (solver/solver.h:38-108) of the last forward run. */
+int gb_export_traces(gb_solver *s, int isrc);
+
+/* Public device buffers (Solver's public members, solver/solver.h:122-156). */
+float *gb_solver_ptr(gb_solver *s, int which);
+int gb_solver_dims(const gb_solver *s, int *nx, int *nz, int *nt, int *nsrc, int *nrec);
+int gb_solver_steps(const gb_solver *s, float *dx, float *dz, float *dt);
+
+/* Batched extension of runForward/runAdjoint: n shots propagate together in
+ * one launch per time step (CUDA-graph captured). Shot b of the call uses
+ * batch slot b; its traces/adjoint sources are gb_slot_ptr(s, b, GB_OUT_*),
+ * gb_slot_ptr(s, b, GB_ADSTF_*). n must not exceed the batch capacity. The
+ * adjoint batch accumulates every slot into GB_K_*. */
+int gb_run_forward_batch(gb_solver *s, const int *isrc, int n);
+int gb_run_adjoint_batch(gb_solver *s, const int *isrc, int n);
+float *gb_slot_ptr(gb_solver *s, int slot, int which);
+int gb_solver_batch_capacity(gb_solver *s);
+/* Runtime options: "batch" (slots, 0 = from the HBM budget), "graphs" (0/1),
+ * "ckpt" (0 FP32, 1 BF16, 2 FP16), "tile" (0 autotune, 1..5 fixed),
+ * "hbm_budget_gb". Options change no numerical result except "ckpt". */
+int gb_solver_set_option(gb_solver *s, const char *key, double value);
+
+/* Timing of the solver since the last reset (CUDA events on the solver's
+ * stream). step_ms / step_launches: fused step kernels timed in windows of
+ * consecutive launches; launches: kernels (or graph kernel nodes) enqueued. */
+typedef struct {
+    double forward_ms, adjoint_ms, misfit_ms, filter_ms;
+    double step_ms;
+    long long step_launches;
+    long long launches;
+    long long cell_updates;
+    int tile_tz, tile_tx, batch_capacity;
+} gb_stats;
+int gb_solver_stats(gb_solver *s, gb_stats *out, int reset);
+
+/* ------------------------------------------------------------------ Filter
+ * Replaces class Filter / GaussianFilter (filter/filter.h:3-15,
+ * filter/gaussian.h:37-61), selected by filter = 0. The smoothing is the
+ * reference's: one-sided (causal) Gaussian weights, normalised by their own
+ * partial sums (filter/gaussian.h:4-36). */
+typedef struct gb_filter gb_filter;
+gb_filter *gb_filter_create(int nx, int nz, int sigma);
+/* GaussianFilter::apply on a device array float[nx*nz]. */
+int gb_filter_apply(gb_filter *f, float *d_data);
+void gb_filter_destroy(gb_filter *f);
+
+/* ------------------------------------------------------------------ Misfit
+ * Replaces class Misfit (misfit/misfit.h:3-153) with WaveformMisfit
+ * (misfit = 0, misfit/waveform.h) and EnvelopeMisfit (misfit = 1,
+ * misfit/envelope.h). Sums are FP64. */
+typedef struct gb_misfit gb_misfit;
+/* Misfit::init (misfit/misfit.h:91-151): filter may be NULL (then one is made
+ * from filter_sigma when filter == 0); observed traces are read from
+ * traces/*.su when trace_file != 0, else generated on model_true; finally
+ * model_init is imported. */
+gb_misfit *gb_misfit_create(const gb_config *cfg, gb_solver *s, gb_filter *f);
+/* Same without files: observed traces from host arrays [nsrc][nrec][nt] per
+ * component (NULL for unused components); the current model is kept. */
+gb_misfit *gb_misfit_create_obs(int type, gb_solver *s, gb_filter *f, const float *obs_x, const float *obs_y,
+                                const float *obs_z);
+/* Replaces the observed traces of every shot, host arrays as above. */
+int gb_misfit_set_obs(gb_misfit *m, const float *obs_x, const float *obs_y, const float *obs_z);
+/* Misfit::run (misfit/misfit.h:15-51): all shots, batched; with kernel != 0
+ * also the adjoint kernels, then the filter on k_lambda, k_mu, k_rho. */
+int gb_misfit_run(gb_misfit *m, int kernel, int snapshot, double *value);
+/* Per-trace misfit values of the last run, [nsrc][nrec][ncomp]. */
+int gb_misfit_trace_values(gb_misfit *m, double *out, size_t n);
+void gb_misfit_destroy(gb_misfit *m);
+
+/* --------------------------------------------------------------- Optimizer
+ * Replaces class Optimizer (optimizer/optimizer.h) with NLCG (optimizer = 0,
+ * optimizer/nlcg.h) and L-BFGS (optimizer = 1, optimizer/lbfgs.h). Dot
+ * products, norms and line-search quantities are FP64 on the GPU; the L-BFGS
+ * history stays in device memory. */
+typedef struct gb_optimizer gb_optimizer;
+gb_optimizer *gb_optimizer_create(const gb_config *cfg, gb_solver *s, gb_misfit *m);
+/* Optimizer::run (optimizer/optimizer.h:428-467), same stdout lines. */
+int gb_optimizer_run(gb_optimizer *o);
+/* Misfit history of the last run: value of each accepted iteration. */
+int gb_optimizer_history(gb_optimizer *o, double *out, int n);
+void gb_optimizer_destroy(gb_optimizer *o);
+
+/* -------------------------------------------------------------- utilities */
+/* FP64 reductions over device float arrays (replace cublasSdot/Isamax/Snrm2
+ * of lib/device.h:178-192). */
+int gb_dot64(const float *d_a, const float *d_b, size_t n, double *out);
+int gb_amax64(const float *d_a, size_t n, double *out);
+/* Plain device memory and copies for FFI callers that hold no CUDA runtime
+ * of their own (the reference allocates with device::create,
+ * lib/device.h:99-111). */
+void *gb_device_malloc(size_t bytes);
+int gb_device_free(void *d_ptr);
+int gb_memcpy_d2h(void *dst, const void *src, size_t bytes);
+int gb_memcpy_h2d(void *dst, const void *src, size_t bytes);
+int gb_device_sync(void);
+int gb_device_count(void);
+/* Pinned host memory (cudaMallocHost) for staging host<->device copies. */
+void *gb_host_malloc(size_t bytes);
+int gb_host_free(void *h_ptr);
+/* Makes `device` current for the calling thread (one process per GPU). */
+int gb_device_select(int device);
+/* CUDA-event timer on the solver's stream: begin != 0 records the start;
+ * begin == 0 records the stop, waits for it and writes the elapsed ms. */
+int gb_solver_timer(gb_solver *s, int begin, double *ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBFWI_H */

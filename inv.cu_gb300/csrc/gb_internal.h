@@ -1,0 +1,115 @@
+// Internal types shared by the CUDA kernels and the host runtime of libgbfwi.
+//
+// Grid layout everywhere is the reference's: float[nx*nz], k = i*nz + j, z
+// (depth) contiguous (lib/device.h:38-40). Wavefields use the same layout so
+// the model, kernel and trace buffers can be handed to callers unchanged.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+namespace gb {
+
+// Number of state arrays per wave system in one slot. Stress and velocity are
+// ping-ponged (the fused step reads time level n and writes n+1 into the
+// other buffer, so neighbouring tiles never see a half-updated field);
+// displacement is updated in place (it is only read at its own cell).
+enum FieldPsv { VX0, VX1, VZ0, VZ1, SXX0, SXX1, SZZ0, SZZ1, SXZ0, SXZ1, UX, UZ, NPSV };
+enum FieldSh { VY0, VY1, SXY0, SXY1, SZY0, SZY1, UY, NSH };
+
+// Checkpoint storage precision.
+enum CkptPrec { CKPT_F32 = 0, CKPT_BF16 = 1, CKPT_F16 = 2 };
+
+// One shot being propagated: everything a step kernel needs, in device
+// memory. A batch is an array of slots; blockIdx.y selects the slot.
+struct Slot {
+    int nx, nz, nt;
+    int tiles_z, tiles_x;
+    int active;
+    float dt;
+    float c9x, c24x, c9z, c24z;  // 9/(8h) and 1/(24h) for h = dx, dz
+    const float *lambda, *mu, *rho;
+    const float *ax, *az;  // absorbing profiles: ab(i,j) = ax[i] * az[j]
+    float *psv[NPSV];      // P-SV state (null when the slot has no P-SV)
+    float *sh[NSH];        // SH state (null when the slot has no SH)
+    // injection (forward sources or adjoint receivers): packed tile CSR
+    const int *inj;
+    const float *inj_x, *inj_y, *inj_z;  // trace data, value = inj_c[trace*nt + it]
+    // recording (receivers): packed tile CSR over owned cells
+    const int *rec;
+    float *out_x, *out_y, *out_z;
+    int record_u;
+    // checkpoints: [nsfe][nf][nx*nz] elements of ckpt_prec, scale [nsfe][nf]
+    void *ckpt;
+    float *ckpt_amax;
+    int nsfe, nf, ckpt_prec;
+};
+
+// A group of slots that accumulate into the same sensitivity kernels.
+struct KernelGroup {
+    float *k_lambda, *k_mu, *k_rho;
+    int inv_lambda, inv_mu, inv_rho;
+    int first, count;  // slot range
+    int nx, nz;
+};
+
+// Tile configuration of the fused step kernel.
+struct TileCfg {
+    int tz, tx;
+};
+
+// Packed tile CSR header: [0]=ntiles [1]=nentries [2]=ntraces, then
+// tile_ptr[ntiles+1], local[nentries], tptr[nentries+1], traces[ntraces].
+inline int csr_words(int ntiles, int nent, int ntr) { return 3 + ntiles + 1 + nent + nent + 1 + ntr; }
+
+// ---------------------------------------------------------------- launchers
+// All launchers enqueue on `st` and return cudaGetLastError().
+cudaError_t launch_step(bool psv, TileCfg tc, const Slot *d_slots, int nslots, int max_tiles, int it,
+                        int par, cudaStream_t st);
+cudaError_t launch_ckpt_amax(const Slot *d_slots, int nslots, int n, int isfe, int which_u, bool psv,
+                             int par, cudaStream_t st);
+cudaError_t launch_ckpt_store(const Slot *d_slots, int nslots, int n, int isfe, int which_u, bool psv,
+                              int par, cudaStream_t st);
+cudaError_t launch_interaction(bool psv, const Slot *d_slots, const KernelGroup *d_groups, int ngroups,
+                               int max_cells, int isfe, float ndt, int par, cudaStream_t st);
+cudaError_t launch_fill(float *p, float v, size_t n, cudaStream_t st);
+cudaError_t launch_mesh2grid(float *lambda, float *mu, float *rho, const float *px, const float *pz,
+                             const float *pa, const float *pb, const float *pr, int npt, float dmax, float dx,
+                             float dz, int nx, int nz, cudaStream_t st);
+cudaError_t launch_scatter_points(float *lambda, float *mu, float *rho, const int *cell_of_point,
+                                  const float *pa, const float *pb, const float *pr, int npt, cudaStream_t st);
+cudaError_t launch_vps2lm(float *lambda, float *mu, const float *rho, size_t n, cudaStream_t st);
+cudaError_t launch_lm2vps(float *vp, float *vs, const float *rho, size_t n, cudaStream_t st);
+cudaError_t launch_axpby(float *c, float ka, const float *a, float kb, const float *b, size_t n,
+                         cudaStream_t st);
+
+// FP64 reductions (gb_reduce.cu). `partial` holds at least reduce_partials()
+// doubles; the result lands in *d_out (device).
+int reduce_partials();
+cudaError_t launch_dot(const float *a, const float *b, size_t n, double *partial, double *d_out,
+                       cudaStream_t st);
+cudaError_t launch_amax(const float *a, size_t n, double *partial, double *d_out, cudaStream_t st);
+
+// Misfits (gb_misfit.cu).
+cudaError_t launch_taper(float *tw, float dt, int nt, cudaStream_t st);
+cudaError_t launch_waveform(const float *syn, const float *obs, const float *tw, float *adstf,
+                            double *trace_val, int ntr, int nt, float sqrt_dt, cudaStream_t st);
+cudaError_t launch_sum_traces(const double *trace_val, int ntr, double *d_out, cudaStream_t st);
+
+// Error state.
+void set_error(const std::string &msg);
+const char *last_error();
+
+}  // namespace gb
+
+#define GB_CUDA_TRY(expr)                                                                      \
+    do {                                                                                       \
+        cudaError_t _e = (expr);                                                               \
+        if (_e != cudaSuccess) {                                                               \
+            ::gb::set_error(std::string(#expr) + ": " + cudaGetErrorString(_e) + " at " +      \
+                            __FILE__ + ":" + std::to_string(__LINE__));                        \
+            return GB_ERR_CUDA;                                                                \
+        }                                                                                      \
+    } while (0)

@@ -1,0 +1,803 @@
+// Solver runtime: the GB300 replacement of FdmSolver (solver/fdm.h:222-613)
+// and the Solver base class (solver/solver.h:7-268).
+//
+// Shots are the batching unit. A batch of n shots owns n slots (wavefields,
+// traces, adjoint sources, forward checkpoints, all resident in HBM); one
+// launch per time step advances all of them. The time loop of a pass is
+// captured once into a CUDA graph per (pass kind, n) and replayed; the
+// per-slot descriptors live in device memory so a replay can serve another
+// set of shots after one small host-to-device copy.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <iostream>
+#include <map>
+#include <vector>
+
+#include "gb_solver.h"
+
+namespace gb {
+
+static const TileCfg kTiles[] = {{32, 32}, {32, 32}, {64, 16}, {32, 16}, {16, 32}, {128, 8}};
+static const int kNumTiles = 5;
+
+// ---------------------------------------------------------------- tables
+// Packs a point set into the tile CSR the step kernel reads. For injection
+// (inj = true) a point is listed for every tile whose velocity region (tile
+// plus 1 cell before and 2 after, in x and z) contains it; for recording it
+// is listed once, for the tile that owns its cell. Points sharing a cell form
+// one entry whose traces are visited in ascending order.
+static std::vector<int> build_csr(const PointSet &p, int nx, int nz, TileCfg tc, bool inj) {
+    const int tz = tc.tz, tx = tc.tx;
+    const int tiles_z = (nz + tz - 1) / tz, tiles_x = (nx + tx - 1) / tx;
+    const int ntiles = tiles_z * tiles_x;
+    const int vz = tz + 3;
+    std::map<int, std::map<int, std::vector<int>>> per;  // tile -> local -> traces
+    for (size_t q = 0; q < p.i.size(); q++) {
+        const int i = p.i[q], j = p.j[q];
+        if (i < 0 || i >= nx || j < 0 || j >= nz) continue;
+        if (inj) {
+            for (int txi = std::max(0, (i - tx - 1) / tx - 1); txi <= std::min(tiles_x - 1, (i + 1) / tx); txi++) {
+                const int i0 = txi * tx;
+                if (i < i0 - 1 || i > i0 + tx + 1) continue;
+                for (int tzi = std::max(0, (j - tz - 1) / tz - 1); tzi <= std::min(tiles_z - 1, (j + 1) / tz);
+                     tzi++) {
+                    const int j0 = tzi * tz;
+                    if (j < j0 - 1 || j > j0 + tz + 1) continue;
+                    const int local = (i - (i0 - 1)) * vz + (j - (j0 - 1));
+                    per[txi * tiles_z + tzi][local].push_back(p.trace[q]);
+                }
+            }
+        } else {
+            const int txi = i / tx, tzi = j / tz;
+            const int local = (i - txi * tx) * tz + (j - tzi * tz);
+            per[txi * tiles_z + tzi][local].push_back(p.trace[q]);
+        }
+    }
+    int nent = 0, ntr = 0;
+    for (auto &t : per) {
+        nent += (int)t.second.size();
+        for (auto &e : t.second) ntr += (int)e.second.size();
+    }
+    std::vector<int> out(csr_words(ntiles, nent, ntr));
+    out[0] = ntiles;
+    out[1] = nent;
+    out[2] = ntr;
+    int *tile_ptr = out.data() + 3;
+    int *local = tile_ptr + ntiles + 1;
+    int *tptr = local + nent;
+    int *traces = tptr + nent + 1;
+    int e = 0, t = 0;
+    auto it = per.begin();
+    for (int tile = 0; tile < ntiles; tile++) {
+        tile_ptr[tile] = e;
+        if (it != per.end() && it->first == tile) {
+            for (auto &ent : it->second) {
+                std::vector<int> trs = ent.second;
+                std::sort(trs.begin(), trs.end());
+                local[e] = ent.first;
+                tptr[e] = t;
+                for (int v : trs) traces[t++] = v;
+                e++;
+            }
+            ++it;
+        }
+    }
+    tile_ptr[ntiles] = e;
+    tptr[nent] = t;
+    return out;
+}
+
+// ---------------------------------------------------------------- source
+// RickerSource::create + Source::init (source/ricker.h:5-21,
+// source/source.h:17-37), host float arithmetic.
+static void ricker(int nt, float dt, const float *cfg, float *sx, float *sy, float *sz) {
+    const float pi = 3.1415927f;
+    const float f0 = cfg[0], t0 = cfg[1], angle = cfg[2], amp = cfg[3];
+    std::vector<float> s(nt);
+    float amax = 0;
+    for (int it = 0; it < nt; it++) {
+        float t = (float)(size_t)it * dt - t0;
+        float pft = pi * f0 * t;
+        s[it] = -t * expf(-pft * pft);
+        if (fabsf(s[it]) > amax) amax = fabsf(s[it]);
+    }
+    if (amax > 0)
+        for (int it = 0; it < nt; it++) s[it] /= amax;
+    for (int it = 0; it < nt; it++) {
+        sx[it] = amp * s[it] * cosf(angle);
+        sy[it] = amp * s[it];
+        sz[it] = amp * s[it] * sinf(angle);
+    }
+}
+
+// calcIdx (solver/fdm.h:44-47).
+static int calc_idx(float c, float L, int n) { return (int)((double)(c / L * (float)(n - 1)) + 0.5); }
+
+// initAbsbound (solver/fdm.h:48-74) as two 1-D profiles: the product over
+// the left/right edges depends on i only, bottom/top on j only, and
+// ab(i,j) = ax[i] * az[j].
+static void absorbing_profiles(int nx, int nz, int w, float alpha, bool l, bool r, bool b, bool t,
+                               std::vector<float> &ax, std::vector<float> &az) {
+    ax.assign(nx, 1.f);
+    az.assign(nz, 1.f);
+    for (int i = 0; i < nx; i++) {
+        if (l && i + 1 < w) ax[i] *= expf(-powf(alpha * (float)(w - i - 1), 2));
+        if (r && i > nx - w) ax[i] *= expf(-powf(alpha * (float)(w + i - nx), 2));
+    }
+    for (int j = 0; j < nz; j++) {
+        if (b && j > nz - w) az[j] *= expf(-powf(alpha * (float)(w + j - nz), 2));
+        if (t && j + 1 < w) az[j] *= expf(-powf(alpha * (float)(w - j - 1), 2));
+    }
+}
+
+// ---------------------------------------------------------------- init
+int Solver::init(const Config &cfg, int nx_, int nz_, float xmax_, float zmax_) {
+    path = cfg.path;
+    dt = cfg.fv("dt");
+    nt = cfg.iv("nt");
+    sfe = cfg.iv("sfe");
+    wfe = cfg.iv("wfe");
+    wae = cfg.iv("wae");
+    sh = cfg.iv("sh") != 0;
+    psv = cfg.iv("psv") != 0;
+    mode = cfg.iv("mode");
+    adj = mode == 0 || mode == 2;
+    trace_type = cfg.iv("trace_type");
+    model_type = cfg.iv("model_type");
+    abs_alpha = cfg.fv("abs_alpha");
+    abs_width = cfg.iv("abs_width");
+    abs_left = cfg.iv("abs_left") != 0;
+    abs_top = cfg.iv("abs_top") != 0;
+    abs_right = cfg.iv("abs_right") != 0;
+    abs_bottom = cfg.iv("abs_bottom") != 0;
+    inv_lambda = cfg.iv("inv_lambda") != 0;
+    inv_mu = cfg.iv("inv_mu") != 0;
+    inv_rho = cfg.iv("inv_rho") != 0;
+    if (cfg.has("batch")) opt_batch = cfg.iv("batch");
+    if (cfg.has("graphs")) opt_graphs = cfg.iv("graphs") != 0;
+    if (cfg.has("ckpt_precision")) opt_ckpt = cfg.iv("ckpt_precision");
+    if (cfg.has("tile")) opt_tile = cfg.iv("tile");
+    nx = nx_;
+    nz = nz_;
+    xmax = xmax_;
+    zmax = zmax_;
+    if (nx < 1 || nz < 1 || nt < 1) {
+        set_error("solver: grid and nt must be positive (nx=" + std::to_string(nx) + " nz=" + std::to_string(nz) +
+                  " nt=" + std::to_string(nt) + ")");
+        return GB_ERR_ARG;
+    }
+    if (!sh && !psv) {
+        set_error("solver: neither sh nor psv is enabled");
+        return GB_ERR_ARG;
+    }
+    if ((size_t)nx * nz > (size_t)INT32_MAX / 4) {
+        set_error("solver: grid too large");
+        return GB_ERR_ARG;
+    }
+    dx = xmax / (float)(nx - 1);
+    dz = zmax / (float)(nz - 1);
+    nsfe = sfe > 0 ? nt / sfe : 0;
+    if (opt_ckpt < CKPT_F32 || opt_ckpt > CKPT_F16) opt_ckpt = CKPT_F32;
+    if (opt_tile < 0 || opt_tile > kNumTiles) opt_tile = 0;
+
+    nsrc = (int)cfg.src.size();
+    nrec = (int)cfg.rec.size();
+    for (auto &s : cfg.src) {
+        src_x.push_back(s[0]);
+        src_z.push_back(s[1]);
+        src_xi.push_back(calc_idx(s[0], xmax, nx));
+        src_zi.push_back(calc_idx(s[1], zmax, nz));
+    }
+    for (auto &r : cfg.rec) {
+        rec_x.push_back(r[0]);
+        rec_z.push_back(r[1]);
+        rec_xi.push_back(calc_idx(r[0], xmax, nx));
+        rec_zi.push_back(calc_idx(r[1], zmax, nz));
+    }
+    for (int q = 0; q < nsrc; q++)
+        if ((int)cfg.src[q][2] != 0) {
+            set_error("solver: source type " + std::to_string((int)cfg.src[q][2]) + " (only 0, Ricker)");
+            return GB_ERR_ARG;
+        }
+
+    GB_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    for (cudaEvent_t *e : {&ev_pass0, &ev_pass1, &ev_win0, &ev_win1}) GB_CUDA_TRY(cudaEventCreate(e));
+
+    const size_t n = ncell();
+    GB_CUDA_TRY(cudaMalloc(&lambda, n * 4));
+    GB_CUDA_TRY(cudaMalloc(&mu, n * 4));
+    GB_CUDA_TRY(cudaMalloc(&rho, n * 4));
+    GB_CUDA_TRY(cudaMemset(lambda, 0, n * 4));
+    GB_CUDA_TRY(cudaMemset(mu, 0, n * 4));
+    GB_CUDA_TRY(cudaMemset(rho, 0, n * 4));
+    if (adj) {
+        GB_CUDA_TRY(cudaMalloc(&k_lambda, n * 4));
+        GB_CUDA_TRY(cudaMalloc(&k_mu, n * 4));
+        GB_CUDA_TRY(cudaMalloc(&k_rho, n * 4));
+        GB_CUDA_TRY(cudaMemset(k_lambda, 0, n * 4));
+        GB_CUDA_TRY(cudaMemset(k_mu, 0, n * 4));
+        GB_CUDA_TRY(cudaMemset(k_rho, 0, n * 4));
+    }
+    // source time functions
+    std::vector<float> hs[3];
+    for (int c = 0; c < 3; c++) hs[c].assign((size_t)std::max(nsrc, 1) * nt, 0.f);
+    for (int is = 0; is < nsrc; is++)
+        ricker(nt, dt, &cfg.src[is][3], &hs[0][(size_t)is * nt], &hs[1][(size_t)is * nt], &hs[2][(size_t)is * nt]);
+    for (int c = 0; c < 3; c++) {
+        GB_CUDA_TRY(cudaMalloc(&stf[c], hs[c].size() * 4));
+        GB_CUDA_TRY(cudaMemcpy(stf[c], hs[c].data(), hs[c].size() * 4, cudaMemcpyHostToDevice));
+    }
+    std::vector<float> hax, haz;
+    absorbing_profiles(nx, nz, abs_width, abs_alpha, abs_left, abs_right, abs_bottom, abs_top, hax, haz);
+    GB_CUDA_TRY(cudaMalloc(&ax, nx * 4));
+    GB_CUDA_TRY(cudaMalloc(&az, nz * 4));
+    GB_CUDA_TRY(cudaMemcpy(ax, hax.data(), nx * 4, cudaMemcpyHostToDevice));
+    GB_CUDA_TRY(cudaMemcpy(az, haz.data(), nz * 4, cudaMemcpyHostToDevice));
+    GB_CUDA_TRY(cudaMalloc(&d_group, sizeof(KernelGroup)));
+    GB_CUDA_TRY(cudaMallocHost(&h_group, sizeof(KernelGroup)));
+    stats = gb_stats{};
+    return GB_OK;
+}
+
+void Solver::release() {
+    if (st) cudaStreamSynchronize(st);
+    invalidate_graphs();
+    for (auto &b : slots) {
+        cudaFree(b.state);
+        for (int c = 0; c < 3; c++) {
+            cudaFree(b.out[c]);
+            cudaFree(b.adstf[c]);
+        }
+        cudaFree(b.ckpt);
+        cudaFree(b.amax);
+    }
+    slots.clear();
+    for (float *p : {lambda, mu, rho, k_lambda, k_mu, k_rho, stf[0], stf[1], stf[2], ax, az}) cudaFree(p);
+    for (int q = 0; q < 3; q++) {
+        cudaFree(d_slots[q]);
+        cudaFreeHost(h_slots[q]);
+    }
+    cudaFree(d_tune);
+    cudaFree(d_group);
+    cudaFreeHost(h_group);
+    cudaFree(d_csr);
+    for (cudaEvent_t e : {ev_pass0, ev_pass1, ev_win0, ev_win1, ev_t0, ev_t1})
+        if (e) cudaEventDestroy(e);
+    if (st) cudaStreamDestroy(st);
+    st = nullptr;
+}
+
+void Solver::invalidate_graphs() {
+    for (auto &g : graphs) cudaGraphExecDestroy(g.second.exec);
+    graphs.clear();
+}
+
+// ---------------------------------------------------------------- model
+int Solver::set_model_points(int npt, const float *px, const float *pz, const float *pa, const float *pb,
+                             const float *pr) {
+    if (npt <= 0 || !px || !pz || !pa || !pb || !pr) {
+        set_error("model: empty point set");
+        return GB_ERR_ARG;
+    }
+    const size_t n = ncell();
+    // Fast path: when every cell has a model point at distance exactly 0
+    // (all shipped examples store the grid itself), the reference's
+    // nearest-point search (mesh2grid, solver/fdm.h:4-24) returns the first
+    // such point, because 0 is the minimum and the comparison is strict.
+    std::vector<int> first(n, -1);
+    size_t hit = 0;
+    for (int l = 0; l < npt; l++) {
+        const long ii = lrintf(px[l] / dx), jj = lrintf(pz[l] / dz);
+        for (long i = ii - 1; i <= ii + 1; i++) {
+            for (long j = jj - 1; j <= jj + 1; j++) {
+                if (i < 0 || j < 0 || i >= nx || j >= nz) continue;
+                const float ddx = (float)i * dx - px[l], ddz = (float)j * dz - pz[l];
+                if (ddx * ddx + ddz * ddz == 0.f) {
+                    int &f = first[(size_t)i * nz + j];
+                    if (f < 0) {
+                        f = l;
+                        hit++;
+                    }
+                }
+            }
+        }
+    }
+    if (hit == n) {
+        std::vector<float> h[3];
+        for (auto &v : h) v.resize(n);
+        for (size_t k = 0; k < n; k++) {
+            h[0][k] = pa[first[k]];
+            h[1][k] = pb[first[k]];
+            h[2][k] = pr[first[k]];
+        }
+        GB_CUDA_TRY(cudaMemcpyAsync(lambda, h[0].data(), n * 4, cudaMemcpyHostToDevice, st));
+        GB_CUDA_TRY(cudaMemcpyAsync(mu, h[1].data(), n * 4, cudaMemcpyHostToDevice, st));
+        GB_CUDA_TRY(cudaMemcpyAsync(rho, h[2].data(), n * 4, cudaMemcpyHostToDevice, st));
+        GB_CUDA_TRY(cudaStreamSynchronize(st));
+    } else {
+        float *d[5];
+        const float *hsrc[5] = {px, pz, pa, pb, pr};
+        for (int q = 0; q < 5; q++) {
+            GB_CUDA_TRY(cudaMalloc(&d[q], (size_t)npt * 4));
+            GB_CUDA_TRY(cudaMemcpyAsync(d[q], hsrc[q], (size_t)npt * 4, cudaMemcpyHostToDevice, st));
+        }
+        const float dmax = xmax * xmax + zmax * zmax;
+        GB_CUDA_TRY(launch_mesh2grid(lambda, mu, rho, d[0], d[1], d[2], d[3], d[4], npt, dmax, dx, dz, nx, nz, st));
+        GB_CUDA_TRY(cudaStreamSynchronize(st));
+        for (int q = 0; q < 5; q++) cudaFree(d[q]);
+    }
+    if (model_type == 0) {
+        GB_CUDA_TRY(launch_vps2lm(lambda, mu, rho, n, st));
+        GB_CUDA_TRY(cudaStreamSynchronize(st));
+    }
+    return GB_OK;
+}
+
+int Solver::import_model(bool model_true) {
+    const std::string dir = path + "/" + (model_true ? "model_true" : "model_init") + "/proc000000_";
+    const char *names0[5] = {"x", "z", "vp", "vs", "rho"};
+    const char *names1[5] = {"x", "z", "lambda", "mu", "rho"};
+    std::vector<float> v[5];
+    for (int q = 0; q < 5; q++) {
+        int rc = read_bin(dir + (model_type ? names1[q] : names0[q]) + ".bin", v[q]);
+        if (rc) return rc;
+        if (model_npt && (int)v[q].size() != model_npt) {
+            set_error("error: invalid model (" + dir + (model_type ? names1[q] : names0[q]) + ".bin has " +
+                      std::to_string(v[q].size()) + " points, expected " + std::to_string(model_npt) + ")");
+            return GB_ERR_MODEL;
+        }
+    }
+    return set_model_points((int)v[0].size(), v[0].data(), v[1].data(), v[2].data(), v[3].data(), v[4].data());
+}
+
+// ---------------------------------------------------------------- slots
+size_t Solver::slot_bytes(int prec) const {
+    const size_t n = ncell();
+    size_t b = ((sh ? NSH : 0) + (psv ? NPSV : 0)) * n * 4;
+    const int ncomp = (sh ? 1 : 0) + (psv ? 2 : 0);
+    b += (size_t)ncomp * nrec * nt * 4 * (adj ? 2 : 1);
+    if (adj && nsfe) b += (size_t)nsfe * nf() * n * (prec == CKPT_F32 ? 4 : 2) + (size_t)nsfe * nf() * 4;
+    return b;
+}
+
+int Solver::ensure_slots(int n) {
+    if (capacity == 0) {
+        size_t freeb = 0, totalb = 0;
+        GB_CUDA_TRY(cudaMemGetInfo(&freeb, &totalb));
+        double budget = opt_budget_gb > 0 ? opt_budget_gb * 1e9 : 0.85 * (double)freeb;
+        long cap = (long)(budget / (double)slot_bytes(opt_ckpt));
+        cap = std::min<long>(cap, std::max(nsrc, 1));
+        cap = std::min<long>(cap, 256);
+        if (opt_batch > 0) cap = std::min<long>(cap, opt_batch);
+        if (cap < 1) {
+            set_error("solver: one shot needs " + std::to_string(slot_bytes(opt_ckpt)) +
+                      " bytes, more than the HBM budget");
+            return GB_ERR_BUDGET;
+        }
+        capacity = (int)cap;
+        for (int q = 0; q < 3; q++) {
+            GB_CUDA_TRY(cudaMalloc(&d_slots[q], sizeof(Slot) * capacity));
+            GB_CUDA_TRY(cudaMallocHost(&h_slots[q], sizeof(Slot) * capacity));
+            memset(h_slots[q], 0, sizeof(Slot) * capacity);
+        }
+        GB_CUDA_TRY(cudaMalloc(&d_tune, sizeof(Slot) * capacity));
+        stats.batch_capacity = capacity;
+    }
+    if (n > capacity) {
+        set_error("solver: batch of " + std::to_string(n) + " exceeds capacity " + std::to_string(capacity));
+        return GB_ERR_BUDGET;
+    }
+    const size_t nc = ncell();
+    while ((int)slots.size() < n) {
+        SlotBuf b;
+        b.state_floats = ((sh ? NSH : 0) + (psv ? NPSV : 0)) * nc;
+        GB_CUDA_TRY(cudaMalloc(&b.state, b.state_floats * 4));
+        const size_t tr = (size_t)nrec * nt;
+        for (int c = 0; c < 3; c++) {
+            const bool used = c == 1 ? sh : psv;
+            if (!used || tr == 0) continue;
+            GB_CUDA_TRY(cudaMalloc(&b.out[c], tr * 4));
+            GB_CUDA_TRY(cudaMemset(b.out[c], 0, tr * 4));
+            if (adj) {
+                GB_CUDA_TRY(cudaMalloc(&b.adstf[c], tr * 4));
+                GB_CUDA_TRY(cudaMemset(b.adstf[c], 0, tr * 4));
+            }
+        }
+        slots.push_back(b);
+    }
+    if (adj && nsfe) {
+        for (int q = 0; q < n; q++) {
+            SlotBuf &b = slots[q];
+            if (b.ckpt_prec == opt_ckpt) continue;
+            cudaFree(b.ckpt);
+            cudaFree(b.amax);
+            const size_t elems = (size_t)nsfe * nf() * nc;
+            GB_CUDA_TRY(cudaMalloc(&b.ckpt, elems * (opt_ckpt == CKPT_F32 ? 4 : 2)));
+            GB_CUDA_TRY(cudaMalloc(&b.amax, (size_t)nsfe * nf() * 4));
+            b.ckpt_prec = opt_ckpt;
+            invalidate_graphs();
+        }
+    }
+    return GB_OK;
+}
+
+int Solver::ensure_tables() {
+    if (d_csr && tile_id == (opt_tile ? opt_tile : tile_id) && tile_id != 0) return GB_OK;
+    if (opt_tile) tile_id = opt_tile;
+    if (tile_id == 0) tile_id = 1;
+    tile = kTiles[tile_id];
+    std::vector<int> all;
+    auto add = [&](const std::vector<int> &v) {
+        size_t off = all.size();
+        all.insert(all.end(), v.begin(), v.end());
+        return off;
+    };
+    src_set.clear();
+    PointSet every;
+    for (int is = 0; is < nsrc; is++) {
+        PointSet one;
+        one.i = {src_xi[is]};
+        one.j = {src_zi[is]};
+        one.trace = {is};
+        src_set.push_back(add(build_csr(one, nx, nz, tile, true)));
+        every.i.push_back(src_xi[is]);
+        every.j.push_back(src_zi[is]);
+        every.trace.push_back(is);
+    }
+    super_set = add(build_csr(every, nx, nz, tile, true));
+    PointSet recs;
+    recs.i = rec_xi;
+    recs.j = rec_zi;
+    for (int ir = 0; ir < nrec; ir++) recs.trace.push_back(ir);
+    rec_inj_set = add(build_csr(recs, nx, nz, tile, true));
+    rec_rec_set = add(build_csr(recs, nx, nz, tile, false));
+    if (d_csr) {
+        GB_CUDA_TRY(cudaStreamSynchronize(st));
+        cudaFree(d_csr);
+    }
+    csr_words = all.size();
+    GB_CUDA_TRY(cudaMalloc(&d_csr, csr_words * 4));
+    GB_CUDA_TRY(cudaMemcpy(d_csr, all.data(), csr_words * 4, cudaMemcpyHostToDevice));
+    stats.tile_tz = tile.tz;
+    stats.tile_tx = tile.tx;
+    return GB_OK;
+}
+
+int Solver::fill_slots(int kind, const int *shots, int n, bool record_u) {
+    Slot *hs = h_slots[kind];
+    const size_t nc = ncell();
+    for (int b = 0; b < capacity; b++) {
+        Slot &S = hs[b];
+        memset(&S, 0, sizeof(Slot));
+        if (b >= n) continue;
+        const SlotBuf &B = slots[b];
+        S.nx = nx;
+        S.nz = nz;
+        S.nt = nt;
+        S.tiles_z = (nz + tile.tz - 1) / tile.tz;
+        S.tiles_x = (nx + tile.tx - 1) / tile.tx;
+        S.active = 1;
+        S.dt = dt;
+        S.c9x = 9.f / (8.f * dx);
+        S.c24x = 1.f / (24.f * dx);
+        S.c9z = 9.f / (8.f * dz);
+        S.c24z = 1.f / (24.f * dz);
+        S.lambda = lambda;
+        S.mu = mu;
+        S.rho = rho;
+        S.ax = ax;
+        S.az = az;
+        float *p = B.state;
+        if (sh) {
+            for (int f = 0; f < NSH; f++) S.sh[f] = p + (size_t)f * nc;
+            p += (size_t)NSH * nc;
+        }
+        if (psv)
+            for (int f = 0; f < NPSV; f++) S.psv[f] = p + (size_t)f * nc;
+        S.nsfe = nsfe;
+        S.nf = nf();
+        S.ckpt_prec = B.ckpt_prec < 0 ? CKPT_F32 : B.ckpt_prec;
+        if (kind == PASS_ADJ) {
+            S.inj = d_csr + rec_inj_set;
+            S.inj_x = B.adstf[0];
+            S.inj_y = B.adstf[1];
+            S.inj_z = B.adstf[2];
+            S.ckpt = B.ckpt;
+            S.ckpt_amax = B.amax;
+        } else {
+            const int is = shots[b];
+            S.inj = nsrc ? d_csr + (is >= 0 ? src_set[is] : super_set) : nullptr;
+            S.inj_x = stf[0];
+            S.inj_y = stf[1];
+            S.inj_z = stf[2];
+            S.rec = nrec ? d_csr + rec_rec_set : nullptr;
+            S.out_x = B.out[0];
+            S.out_y = B.out[1];
+            S.out_z = B.out[2];
+            S.record_u = record_u;
+            if (kind == PASS_FWD) {
+                S.ckpt = B.ckpt;
+                S.ckpt_amax = B.amax;
+            }
+        }
+    }
+    GB_CUDA_TRY(cudaMemcpyAsync(d_slots[kind], hs, sizeof(Slot) * capacity, cudaMemcpyHostToDevice, st));
+    return GB_OK;
+}
+
+// Enqueues one pass on st (also used inside graph capture).
+int Solver::enqueue_pass(int kind, int n, bool snapshot, int snap_isrc) {
+    const size_t nc = ncell();
+    const Slot *ds = d_slots[kind];
+    for (int b = 0; b < n; b++) GB_CUDA_TRY(cudaMemsetAsync(slots[b].state, 0, slots[b].state_floats * 4, st));
+    const bool ck = kind == PASS_FWD && adj && nsfe > 0;
+    const bool q16 = ck && opt_ckpt != CKPT_F32;
+    if (q16)
+        for (int b = 0; b < n; b++) GB_CUDA_TRY(cudaMemsetAsync(slots[b].amax, 0, (size_t)nsfe * nf() * 4, st));
+    // timing window: consecutive steps with no other kernel between them
+    int w0 = 0, w1 = std::min(nt, 64);
+    if (ck) w1 = std::min(w1, sfe - 1);
+    if (kind == PASS_ADJ) {
+        w0 = std::min(1, nt);
+        w1 = std::min(nt, std::min(w0 + 64, sfe > 0 ? sfe : nt));
+    }
+    if (w1 <= w0) w1 = w0;  // empty window: not timed
+    win_steps = w1 - w0;
+    const int nwave = (sh ? 1 : 0) + (psv ? 1 : 0);
+    int par = 0;
+    const float ndt = (float)sfe * dt;
+    for (int it = 0; it < nt; it++) {
+        int isfe = -1;
+        if (ck && (it + 1) % sfe == 0) isfe = nsfe - (it + 1) / sfe;
+        if (isfe >= 0) {
+            for (int w = 0; w < 2; w++) {
+                const bool wp = w == 1;
+                if (wp ? !psv : !sh) continue;
+                if (q16) GB_CUDA_TRY(launch_ckpt_amax(ds, n, (int)nc, isfe, 1, wp, par, st));
+                GB_CUDA_TRY(launch_ckpt_store(ds, n, (int)nc, isfe, 1, wp, par, st));
+                stats.launches += q16 ? 2 : 1;
+            }
+        }
+        if (it == w0 && win_steps > 0) GB_CUDA_TRY(cudaEventRecord(ev_win0, st));
+        if (sh) GB_CUDA_TRY(launch_step(false, tile, ds, n, max_tiles(), it, par, st));
+        if (psv) GB_CUDA_TRY(launch_step(true, tile, ds, n, max_tiles(), it, par, st));
+        stats.launches += nwave;
+        if (it + 1 == w1 && win_steps > 0) GB_CUDA_TRY(cudaEventRecord(ev_win1, st));
+        par ^= 1;
+        if (isfe >= 0) {
+            for (int w = 0; w < 2; w++) {
+                const bool wp = w == 1;
+                if (wp ? !psv : !sh) continue;
+                if (q16) GB_CUDA_TRY(launch_ckpt_amax(ds, n, (int)nc, isfe, 0, wp, par, st));
+                GB_CUDA_TRY(launch_ckpt_store(ds, n, (int)nc, isfe, 0, wp, par, st));
+                stats.launches += q16 ? 2 : 1;
+            }
+        }
+        if (kind == PASS_ADJ && sfe > 0 && it % sfe == 0) {
+            const int isfe_a = it / sfe;
+            if (sh) GB_CUDA_TRY(launch_interaction(false, ds, d_group, 1, (int)nc, isfe_a, ndt, par, st));
+            if (psv) GB_CUDA_TRY(launch_interaction(true, ds, d_group, 1, (int)nc, isfe_a, ndt, par, st));
+            stats.launches += nwave;
+        }
+        if (snapshot) {
+            int rc = export_snapshot(it, snap_isrc, par);
+            if (rc) return rc;
+        }
+    }
+    last_par = par;
+    stats.cell_updates += (long long)nc * nt * n;
+    return GB_OK;
+}
+
+int Solver::autotune(int n) {
+    // Times every tile shape on the real batch (sources and receivers off,
+    // results discarded) and keeps the fastest; the shape does not change
+    // any computed value.
+    Slot *hs = h_slots[PASS_FWD_NOCKPT];
+    std::vector<Slot> tmp(hs, hs + capacity);
+    for (int b = 0; b < capacity; b++) {
+        tmp[b].inj = nullptr;
+        tmp[b].rec = nullptr;
+    }
+    float best = 1e30f;
+    int best_id = 1;
+    for (int id = 1; id <= kNumTiles; id++) {
+        TileCfg tc = kTiles[id];
+        for (int b = 0; b < n; b++) {
+            tmp[b].tiles_z = (nz + tc.tz - 1) / tc.tz;
+            tmp[b].tiles_x = (nx + tc.tx - 1) / tc.tx;
+        }
+        GB_CUDA_TRY(cudaMemcpyAsync(d_tune, tmp.data(), sizeof(Slot) * capacity, cudaMemcpyHostToDevice, st));
+        const int mt = ((nz + tc.tz - 1) / tc.tz) * ((nx + tc.tx - 1) / tc.tx);
+        const int reps = 8;
+        for (int r = 0; r < 3 + reps; r++) {
+            if (r == 3) GB_CUDA_TRY(cudaEventRecord(ev_win0, st));
+            if (sh) GB_CUDA_TRY(launch_step(false, tc, d_tune, n, mt, r, r & 1, st));
+            if (psv) GB_CUDA_TRY(launch_step(true, tc, d_tune, n, mt, r, r & 1, st));
+        }
+        GB_CUDA_TRY(cudaEventRecord(ev_win1, st));
+        GB_CUDA_TRY(cudaEventSynchronize(ev_win1));
+        float ms = 0;
+        GB_CUDA_TRY(cudaEventElapsedTime(&ms, ev_win0, ev_win1));
+        if (ms < best) {
+            best = ms;
+            best_id = id;
+        }
+    }
+    tile_id = best_id;
+    opt_tile = 0;
+    return GB_OK;
+}
+
+int Solver::run_pass(int kind, int n, bool snapshot, int snap_isrc) {
+    GB_CUDA_TRY(cudaEventRecord(ev_pass0, st));
+    if (opt_graphs && !snapshot) {
+        auto key = std::make_pair(kind, n);
+        auto g = graphs.find(key);
+        if (g == graphs.end()) {
+            const long long l0 = stats.launches, c0 = stats.cell_updates;
+            GB_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            int rc = enqueue_pass(kind, n, false, -1);
+            cudaGraph_t graph = nullptr;
+            cudaError_t e = cudaStreamEndCapture(st, &graph);
+            GraphInfo info;
+            info.launches = stats.launches - l0;
+            info.win_steps = win_steps;
+            stats.launches = l0;
+            stats.cell_updates = c0;
+            if (rc) {
+                if (graph) cudaGraphDestroy(graph);
+                return rc;
+            }
+            GB_CUDA_TRY(e);
+            e = cudaGraphInstantiate(&info.exec, graph, 0);
+            cudaGraphDestroy(graph);
+            GB_CUDA_TRY(e);
+            g = graphs.emplace(key, info).first;
+        }
+        GB_CUDA_TRY(cudaGraphLaunch(g->second.exec, st));
+        stats.launches += g->second.launches;
+        stats.cell_updates += (long long)ncell() * nt * n;
+        win_steps = g->second.win_steps;
+        last_par = nt & 1;
+    } else {
+        int rc = enqueue_pass(kind, n, snapshot, snap_isrc);
+        if (rc) return rc;
+    }
+    GB_CUDA_TRY(cudaEventRecord(ev_pass1, st));
+    GB_CUDA_TRY(cudaStreamSynchronize(st));
+    float ms = 0;
+    GB_CUDA_TRY(cudaEventElapsedTime(&ms, ev_pass0, ev_pass1));
+    if (kind == PASS_ADJ)
+        stats.adjoint_ms += ms;
+    else
+        stats.forward_ms += ms;
+    if (win_steps > 0) {
+        float wm = 0;
+        if (cudaEventElapsedTime(&wm, ev_win0, ev_win1) == cudaSuccess) {
+            stats.step_ms += wm;
+            stats.step_launches += win_steps;
+        } else {
+            (void)cudaGetLastError();  // timing is best effort; clear the error
+        }
+    }
+    return GB_OK;
+}
+
+int Solver::forward(const int *shots, int n, bool ckpt_on, bool record_u, bool snapshot) {
+    if (n < 1) return GB_OK;
+    for (int b = 0; b < n; b++)
+        if (shots[b] >= nsrc || (shots[b] < 0 && nsrc == 0)) {
+            set_error("forward: shot index " + std::to_string(shots[b]) + " out of range");
+            return GB_ERR_ARG;
+        }
+    int rc = ensure_slots(n);
+    if (rc) return rc;
+    if (opt_tile == 0 && tile_id == 0) {
+        rc = ensure_tables();
+        if (rc) return rc;
+        rc = fill_slots(PASS_FWD_NOCKPT, shots, n, record_u);
+        if (rc) return rc;
+        rc = autotune(n);
+        if (rc) return rc;
+        cudaFree(d_csr);
+        d_csr = nullptr;
+        invalidate_graphs();
+    }
+    if (opt_tile && opt_tile != tile_id) {
+        cudaStreamSynchronize(st);
+        cudaFree(d_csr);
+        d_csr = nullptr;
+        invalidate_graphs();
+    }
+    rc = ensure_tables();
+    if (rc) return rc;
+    const int kind = (ckpt_on && adj && nsfe) ? PASS_FWD : PASS_FWD_NOCKPT;
+    rc = fill_slots(kind, shots, n, record_u);
+    if (rc) return rc;
+    last_forward_n = n;
+    return run_pass(kind, n, snapshot, -1);
+}
+
+int Solver::adjoint(const int *shots, int n, bool snapshot, int snap_isrc) {
+    if (n < 1) return GB_OK;
+    if (!adj) {
+        set_error("adjoint: solver was created for a mode without adjoint (mode 0 or 2 needed)");
+        return GB_ERR_STATE;
+    }
+    if (sfe <= 0 || nt % sfe != 0) {
+        set_error("adjoint: nt (" + std::to_string(nt) + ") must be a positive multiple of sfe (" +
+                  std::to_string(sfe) + "); the reference reads past its checkpoints otherwise");
+        return GB_ERR_ARG;
+    }
+    int rc = ensure_slots(n);
+    if (rc) return rc;
+    rc = ensure_tables();
+    if (rc) return rc;
+    rc = fill_slots(PASS_ADJ, shots, n, false);
+    if (rc) return rc;
+    KernelGroup &G = *h_group;
+    G.k_lambda = k_lambda;
+    G.k_mu = k_mu;
+    G.k_rho = k_rho;
+    G.inv_lambda = inv_lambda;
+    G.inv_mu = inv_mu;
+    G.inv_rho = inv_rho;
+    G.first = 0;
+    G.count = n;
+    G.nx = nx;
+    G.nz = nz;
+    GB_CUDA_TRY(cudaMemcpyAsync(d_group, h_group, sizeof(KernelGroup), cudaMemcpyHostToDevice, st));
+    return run_pass(PASS_ADJ, n, snapshot, snap_isrc);
+}
+
+int Solver::init_kernels() {
+    if (!adj) return GB_OK;
+    const size_t n = ncell() * 4;
+    GB_CUDA_TRY(cudaMemsetAsync(k_lambda, 0, n, st));
+    GB_CUDA_TRY(cudaMemsetAsync(k_mu, 0, n, st));
+    GB_CUDA_TRY(cudaMemsetAsync(k_rho, 0, n, st));
+    GB_CUDA_TRY(cudaStreamSynchronize(st));
+    return GB_OK;
+}
+
+// ---------------------------------------------------------------- export
+int Solver::export_data(const std::string &comp, const float *d_data, int n) {
+    std::vector<float> h(ncell());
+    GB_CUDA_TRY(cudaMemcpyAsync(h.data(), d_data, ncell() * 4, cudaMemcpyDeviceToHost, st));
+    GB_CUDA_TRY(cudaStreamSynchronize(st));
+    return write_bin(path + "/output/proc" + pad6(n) + "_" + comp + ".bin", h.data(), ncell());
+}
+
+// FdmSolver::exportSnapshot (solver/fdm.h:312-347), slot 0.
+int Solver::export_snapshot(int it, int isrc, int par) {
+    std::string istr;
+    int we = wfe;
+    if (isrc >= 0) {
+        istr = std::to_string(isrc);
+        const size_t digit = std::to_string(nsrc).size();
+        while (istr.size() < digit) istr = "0" + istr;
+        we = wae;
+    }
+    if (!we || (it + 1) % we != 0) return GB_OK;
+    const size_t nc = ncell();
+    float *p = slots[0].state;
+    float *shp = sh ? p : nullptr;
+    float *psp = sh ? p + (size_t)NSH * nc : p;
+    int rc = GB_OK;
+    if (trace_type == 0) {
+        if (sh && !rc) rc = export_data("vy" + istr, shp + (size_t)(VY0 + par) * nc, it + 1);
+        if (psv && !rc) rc = export_data("vx" + istr, psp + (size_t)(VX0 + par) * nc, it + 1);
+        if (psv && !rc) rc = export_data("vz" + istr, psp + (size_t)(VZ0 + par) * nc, it + 1);
+    } else if (trace_type == 1) {
+        if (sh && !rc) rc = export_data("uy" + istr, shp + (size_t)UY * nc, it + 1);
+        if (psv && !rc) rc = export_data("ux" + istr, psp + (size_t)UX * nc, it + 1);
+        if (psv && !rc) rc = export_data("uz" + istr, psp + (size_t)UZ * nc, it + 1);
+    }
+    return rc;
+}
+
+}  // namespace gb

@@ -1,0 +1,126 @@
+// Host runtime of the solver: owns device buffers, batch slots, the tile
+// tables of sources/receivers, captured CUDA graphs and timing.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "gb_config.h"
+#include "gb_internal.h"
+#include "gbfwi.h"
+
+namespace gb {
+
+struct SlotBuf {
+    float *state = nullptr;
+    size_t state_floats = 0;
+    float *out[3] = {nullptr, nullptr, nullptr};
+    float *adstf[3] = {nullptr, nullptr, nullptr};
+    void *ckpt = nullptr;
+    float *amax = nullptr;
+    int ckpt_prec = -1;
+};
+
+struct PointSet {
+    std::vector<int> i, j, trace;
+};
+
+enum PassKind { PASS_FWD = 0, PASS_FWD_NOCKPT = 1, PASS_ADJ = 2 };
+
+struct GraphInfo {
+    cudaGraphExec_t exec = nullptr;
+    long long launches = 0;  // kernels one replay runs
+    int win_steps = 0;       // steps in its timing window
+};
+
+struct Solver {
+    // configuration (Solver::init, solver/solver.h:158-224)
+    std::string path;
+    int nx = 0, nz = 0, nt = 0, sfe = 0, wfe = 0, wae = 0, nsfe = 0;
+    float dx = 0, dz = 0, dt = 0, xmax = 0, zmax = 0;
+    bool sh = false, psv = false, adj = false;
+    int trace_type = 0, model_type = 0, mode = 0;
+    int abs_width = 0;
+    float abs_alpha = 0;
+    bool abs_left = false, abs_right = false, abs_top = false, abs_bottom = false;
+    bool inv_lambda = false, inv_mu = false, inv_rho = false;
+    int nsrc = 0, nrec = 0;
+    int model_npt = 0;
+    std::vector<float> src_x, src_z, rec_x, rec_z;
+    std::vector<int> src_xi, src_zi, rec_xi, rec_zi;
+
+    // options (no effect on results except ckpt precision)
+    int opt_batch = 0;
+    bool opt_graphs = true;
+    int opt_ckpt = CKPT_F32;
+    int opt_tile = 0;  // 0 = autotune
+    double opt_budget_gb = 0;
+
+    // device buffers in the reference layout
+    float *lambda = nullptr, *mu = nullptr, *rho = nullptr;
+    float *k_lambda = nullptr, *k_mu = nullptr, *k_rho = nullptr;
+    float *stf[3] = {nullptr, nullptr, nullptr};
+    float *ax = nullptr, *az = nullptr;
+
+    // batch slots
+    std::vector<SlotBuf> slots;
+    int capacity = 0;
+    Slot *d_slots[3] = {nullptr, nullptr, nullptr};
+    Slot *h_slots[3] = {nullptr, nullptr, nullptr};
+    Slot *d_tune = nullptr;
+    KernelGroup *d_group = nullptr;
+    KernelGroup *h_group = nullptr;
+
+    // tile tables
+    int tile_id = 0;
+    TileCfg tile{32, 32};
+    int *d_csr = nullptr;
+    size_t csr_words = 0;
+    std::vector<size_t> src_set;  // per source
+    size_t super_set = 0, rec_inj_set = 0, rec_rec_set = 0;
+
+    // graphs, keyed by (pass kind, nslots)
+    std::map<std::pair<int, int>, GraphInfo> graphs;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev_pass0 = nullptr, ev_pass1 = nullptr, ev_win0 = nullptr, ev_win1 = nullptr;
+    cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr;  // gb_solver_timer
+    int win_steps = 0;
+    int last_par = 0;
+    int last_forward_n = 0;
+    gb_stats stats{};
+
+    // --- lifecycle
+    int init(const Config &cfg, int nx_, int nz_, float xmax_, float zmax_);
+    void release();
+    // --- model
+    int set_model_points(int npt, const float *x, const float *z, const float *a, const float *b, const float *r);
+    int import_model(bool model_true);
+    // --- passes
+    int ensure_slots(int n);
+    int ensure_tables();
+    int forward(const int *shots, int n, bool ckpt_on, bool record_u, bool snapshot);
+    int adjoint(const int *shots, int n, bool snapshot, int snap_isrc);
+    int init_kernels();
+    // --- helpers
+    size_t ncell() const { return (size_t)nx * nz; }
+    int nf() const { return (sh ? 2 : 0) + (psv ? 4 : 0); }
+    size_t slot_bytes(int prec) const;
+    int fill_slots(int kind, const int *shots, int n, bool record_u);
+    int enqueue_pass(int kind, int n, bool snapshot, int snap_isrc);
+    int run_pass(int kind, int n, bool snapshot, int snap_isrc);
+    int autotune(int n);
+    int export_snapshot(int it, int isrc, int par);
+    int export_data(const std::string &comp, const float *d_data, int n);
+    void invalidate_graphs();
+    int max_tiles() const { return ((nz + tile.tz - 1) / tile.tz) * ((nx + tile.tx - 1) / tile.tx); }
+};
+
+}  // namespace gb
+
+struct gb_solver {
+    gb::Solver s;
+};

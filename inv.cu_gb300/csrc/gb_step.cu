@@ -1,0 +1,508 @@
+// Fused time-step kernels of the staggered-grid velocity-stress solver.
+//
+// One launch advances every slot (shot) of a batch by one time step: the
+// reference's six launches per step (divS, addSTF, updateV, divV, updateS,
+// saveRec; solver/fdm.h:273-294,534-551) become one kernel per wave system.
+//
+// A thread block owns a TZ x TX tile (z contiguous). It
+//   1. stages stress at time n on the tile plus a 3-cell halo in shared memory,
+//   2. computes the stress divergence on the tile plus the velocity halo
+//      (1 cell before, 2 after), adds the source or adjoint-source samples that
+//      fall there, and updates velocity (absorbing factor applied to v only,
+//      solver/fdm.h:150-161) and, on owned cells, displacement,
+//   3. records the receivers it owns, then
+//   4. updates stress on the owned cells from the velocity in shared memory.
+// The velocity halo is recomputed by each neighbouring tile, so one launch
+// needs no grid-wide synchronisation; stress and velocity are ping-ponged
+// between two buffers so no tile reads a neighbour's half-updated values.
+//
+// Derivative guards follow the reference exactly (solver/fdm.h:76-136): the
+// x part of the stress divergence is 0 outside 2 <= i < nx-2, the z part is
+// added only for 2 <= j < nz-2, velocity gradients are 0 outside
+// 1 <= i < nx-2 / 1 <= j < nz-2. The reference's divisions are replaced by
+// multiplications with 9/(8h), 1/(24h) and the reciprocal density; the
+// difference is FP32 round-off (about 1e-6 relative on the golden traces).
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "gb_internal.h"
+
+namespace gb {
+
+constexpr int kThreads = 256;
+
+// Backward-staggered difference at k: 9(a0 - am1)/(8h) - (ap1 - am2)/(24h).
+__device__ __forceinline__ float dminus(float a0, float am1, float ap1, float am2, float c9, float c24) {
+    return fmaf(a0 - am1, c9, -((ap1 - am2) * c24));
+}
+// Forward-staggered difference at k: 9(ap1 - a0)/(8h) - (ap2 - am1)/(24h).
+__device__ __forceinline__ float dplus(float ap1, float a0, float ap2, float am1, float c9, float c24) {
+    return fmaf(ap1 - a0, c9, -((ap2 - am1) * c24));
+}
+
+struct Csr {
+    const int *tile_ptr, *local, *tptr, *traces;
+    __device__ Csr(const int *p) {
+        const int ntiles = p[0], nent = p[1];
+        tile_ptr = p + 3;
+        local = tile_ptr + ntiles + 1;
+        tptr = local + nent;
+        traces = tptr + nent + 1;
+    }
+};
+
+template <bool PSV, int TZ, int TX>
+__global__ void __launch_bounds__(kThreads) k_step(const Slot *__restrict__ slots, int it, int par) {
+    constexpr int NS = PSV ? 3 : 2;  // stress components held in shared memory
+    constexpr int NV = PSV ? 2 : 1;  // velocity components
+    constexpr int RZ = TZ + 6, RX = TX + 6;
+    constexpr int VZ = TZ + 3, VX = TX + 3;
+    __shared__ float s_sig[NS][RX * RZ];
+    __shared__ float s_v[NV][VX * VZ];
+
+    const Slot &S = slots[blockIdx.y];
+    if (!S.active) return;
+    const int nx = S.nx, nz = S.nz;
+    const int tile = blockIdx.x;
+    if (tile >= S.tiles_z * S.tiles_x) return;
+    const int tzi = tile % S.tiles_z, txi = tile / S.tiles_z;
+    const int j0 = tzi * TZ, i0 = txi * TX;
+
+    const float *sig_in[NS];
+    float *sig_out[NS];
+    const float *v_in[NV];
+    float *v_out[NV];
+    float *u[NV];
+    if (PSV) {
+#pragma unroll
+        for (int f = 0; f < NS; f++) {
+            sig_in[f] = S.psv[SXX0 + 2 * f + par];
+            sig_out[f] = S.psv[SXX0 + 2 * f + (par ^ 1)];
+        }
+#pragma unroll
+        for (int f = 0; f < NV; f++) {
+            v_in[f] = S.psv[VX0 + 2 * f + par];
+            v_out[f] = S.psv[VX0 + 2 * f + (par ^ 1)];
+            u[f] = S.psv[UX + f];
+        }
+    } else {
+#pragma unroll
+        for (int f = 0; f < NS; f++) {
+            sig_in[f] = S.sh[SXY0 + 2 * f + par];
+            sig_out[f] = S.sh[SXY0 + 2 * f + (par ^ 1)];
+        }
+        v_in[0] = S.sh[VY0 + par];
+        v_out[0] = S.sh[VY0 + (par ^ 1)];
+        u[0] = S.sh[UY];
+    }
+    const float dt = S.dt, c9x = S.c9x, c24x = S.c24x, c9z = S.c9z, c24z = S.c24z;
+
+    // 1. stress at time n on the tile + 3-cell halo (zero outside the grid;
+    //    those values only feed results the guards discard).
+    for (int e = threadIdx.x; e < RX * RZ; e += kThreads) {
+        const int c = e / RZ, r = e - c * RZ;
+        const int i = i0 - 3 + c, j = j0 - 3 + r;
+        const bool in = (unsigned)i < (unsigned)nx && (unsigned)j < (unsigned)nz;
+        const size_t k = (size_t)i * nz + j;
+#pragma unroll
+        for (int f = 0; f < NS; f++) s_sig[f][e] = in ? __ldg(sig_in[f] + k) : 0.f;
+    }
+    __syncthreads();
+
+    // 2. stress divergence on the velocity region (tile + 1 before, 2 after).
+    auto divergence = [&](int c, int r, int i, int j, float *ds) {
+        const int cc = c + 2, rr = r + 2;
+#define SG(f, dc, dr) s_sig[f][(cc + (dc)) * RZ + rr + (dr)]
+        if (PSV) {
+            float dsx = 0.f, dsz = 0.f;
+            if (i >= 2 && i < nx - 2) {
+                dsx = dminus(SG(0, 0, 0), SG(0, -1, 0), SG(0, 1, 0), SG(0, -2, 0), c9x, c24x);
+                dsz = dminus(SG(2, 0, 0), SG(2, -1, 0), SG(2, 1, 0), SG(2, -2, 0), c9x, c24x);
+            }
+            if (j >= 2 && j < nz - 2) {
+                dsx += dminus(SG(2, 0, 0), SG(2, 0, -1), SG(2, 0, 1), SG(2, 0, -2), c9z, c24z);
+                dsz += dminus(SG(1, 0, 0), SG(1, 0, -1), SG(1, 0, 1), SG(1, 0, -2), c9z, c24z);
+            }
+            ds[0] = dsx;
+            ds[NV - 1] = dsz;
+        } else {
+            float dsy = 0.f;
+            if (i >= 2 && i < nx - 2) dsy = dminus(SG(0, 0, 0), SG(0, -1, 0), SG(0, 1, 0), SG(0, -2, 0), c9x, c24x);
+            if (j >= 2 && j < nz - 2) dsy += dminus(SG(1, 0, 0), SG(1, 0, -1), SG(1, 0, 1), SG(1, 0, -2), c9z, c24z);
+            ds[0] = dsy;
+        }
+#undef SG
+    };
+    auto update_v = [&](int c, int r, int i, int j, const float *ds) {
+        const int e = c * VZ + r;
+        if ((unsigned)i < (unsigned)nx && (unsigned)j < (unsigned)nz) {
+            const size_t k = (size_t)i * nz + j;
+            const float ab = __ldg(S.ax + i) * __ldg(S.az + j);
+            const float rinv = __frcp_rn(__ldg(S.rho + k));
+            const bool own = c >= 1 && c <= TX && r >= 1 && r <= TZ;
+#pragma unroll
+            for (int f = 0; f < NV; f++) {
+                const float vn = ab * fmaf(dt * ds[f], rinv, __ldg(v_in[f] + k));
+                s_v[f][e] = vn;
+                if (own) {
+                    v_out[f][k] = vn;
+                    u[f][k] = u[f][k] + vn * dt;
+                }
+            }
+        } else {
+#pragma unroll
+            for (int f = 0; f < NV; f++) s_v[f][e] = 0.f;
+        }
+    };
+
+    int ninj = 0, inj_first = 0;
+    if (S.inj) {
+        const Csr cs(S.inj);
+        inj_first = cs.tile_ptr[tile];
+        ninj = cs.tile_ptr[tile + 1] - inj_first;
+    }
+    if (ninj == 0) {
+        for (int e = threadIdx.x; e < VX * VZ; e += kThreads) {
+            const int c = e / VZ, r = e - c * VZ;
+            const int i = i0 - 1 + c, j = j0 - 1 + r;
+            float ds[NV];
+            divergence(c, r, i, j, ds);
+            update_v(c, r, i, j, ds);
+        }
+    } else {
+        // Sources in this region: divergence first, then the samples are
+        // added in trace order (solver/fdm.h:163-180), then velocity.
+        for (int e = threadIdx.x; e < VX * VZ; e += kThreads) {
+            const int c = e / VZ, r = e - c * VZ;
+            float ds[NV];
+            divergence(c, r, i0 - 1 + c, j0 - 1 + r, ds);
+#pragma unroll
+            for (int f = 0; f < NV; f++) s_v[f][e] = ds[f];
+        }
+        __syncthreads();
+        const Csr cs(S.inj);
+        const int nt = S.nt;
+        for (int q = threadIdx.x; q < ninj; q += kThreads) {
+            const int ent = inj_first + q;
+            const int e = cs.local[ent];
+            float a0 = s_v[0][e], a1 = s_v[NV - 1][e];
+            for (int t = cs.tptr[ent]; t < cs.tptr[ent + 1]; t++) {
+                const size_t ks = (size_t)cs.traces[t] * nt + it;
+                if (PSV) {
+                    a0 += __ldg(S.inj_x + ks);
+                    a1 += __ldg(S.inj_z + ks);
+                } else {
+                    a0 += __ldg(S.inj_y + ks);
+                }
+            }
+            s_v[0][e] = a0;
+            if (PSV) s_v[NV - 1][e] = a1;
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < VX * VZ; e += kThreads) {
+            const int c = e / VZ, r = e - c * VZ;
+            float ds[NV];
+#pragma unroll
+            for (int f = 0; f < NV; f++) ds[f] = s_v[f][e];
+            update_v(c, r, i0 - 1 + c, j0 - 1 + r, ds);
+        }
+    }
+    __syncthreads();
+
+    // 3. receivers owned by this tile (solver/fdm.h:181-196): u when
+    //    record_u (adjoint-capable runs or trace_type 1), else v.
+    if (S.rec) {
+        const Csr cs(S.rec);
+        const int first = cs.tile_ptr[tile], nrec = cs.tile_ptr[tile + 1] - first;
+        const int nt = S.nt;
+        for (int q = threadIdx.x; q < nrec; q += kThreads) {
+            const int ent = first + q;
+            const int e = cs.local[ent];  // c * TZ + r within the owned tile
+            const int c = e / TZ, r = e - c * TZ;
+            const size_t k = (size_t)(i0 + c) * nz + (j0 + r);
+            const int ev = (c + 1) * VZ + (r + 1);
+            for (int t = cs.tptr[ent]; t < cs.tptr[ent + 1]; t++) {
+                const size_t kr = (size_t)cs.traces[t] * nt + it;
+                if (PSV) {
+                    S.out_x[kr] = S.record_u ? u[0][k] : s_v[0][ev];
+                    S.out_z[kr] = S.record_u ? u[NV - 1][k] : s_v[NV - 1][ev];
+                } else {
+                    S.out_y[kr] = S.record_u ? u[0][k] : s_v[0][ev];
+                }
+            }
+        }
+    }
+
+    // 4. stress update on owned cells (solver/fdm.h:138-149).
+    for (int e = threadIdx.x; e < TX * TZ; e += kThreads) {
+        const int c = e / TZ, r = e - c * TZ;
+        const int i = i0 + c, j = j0 + r;
+        if (i >= nx || j >= nz) continue;
+        const size_t k = (size_t)i * nz + j;
+        const int vc = c + 1, vr = r + 1;
+        const int se = (c + 3) * RZ + (r + 3);
+#define VV(f, dc, dr) s_v[f][(vc + (dc)) * VZ + vr + (dr)]
+        const float m = __ldg(S.mu + k);
+        if (PSV) {
+            float dvxdx = 0.f, dvzdx = 0.f, dvxdz = 0.f, dvzdz = 0.f;
+            if (i >= 1 && i < nx - 2) {
+                dvxdx = dplus(VV(0, 1, 0), VV(0, 0, 0), VV(0, 2, 0), VV(0, -1, 0), c9x, c24x);
+                dvzdx = dplus(VV(1, 1, 0), VV(1, 0, 0), VV(1, 2, 0), VV(1, -1, 0), c9x, c24x);
+            }
+            if (j >= 1 && j < nz - 2) {
+                dvxdz = dplus(VV(0, 0, 1), VV(0, 0, 0), VV(0, 0, 2), VV(0, 0, -1), c9z, c24z);
+                dvzdz = dplus(VV(1, 0, 1), VV(1, 0, 0), VV(1, 0, 2), VV(1, 0, -1), c9z, c24z);
+            }
+            const float l = __ldg(S.lambda + k);
+            const float l2m = l + 2.f * m;
+            sig_out[0][k] = s_sig[0][se] + dt * (l2m * dvxdx + l * dvzdz);
+            sig_out[1][k] = s_sig[1][se] + dt * (l2m * dvzdz + l * dvxdx);
+            sig_out[2][k] = s_sig[2][se] + dt * (m * (dvxdz + dvzdx));
+        } else {
+            float dvydx = 0.f, dvydz = 0.f;
+            if (i >= 1 && i < nx - 2) dvydx = dplus(VV(0, 1, 0), VV(0, 0, 0), VV(0, 2, 0), VV(0, -1, 0), c9x, c24x);
+            if (j >= 1 && j < nz - 2) dvydz = dplus(VV(0, 0, 1), VV(0, 0, 0), VV(0, 0, 2), VV(0, 0, -1), c9z, c24z);
+            sig_out[0][k] = s_sig[0][se] + dt * m * dvydx;
+            sig_out[1][k] = s_sig[1][se] + dt * m * dvydz;
+        }
+#undef VV
+    }
+}
+
+template <bool PSV>
+static cudaError_t launch_step_t(TileCfg tc, const Slot *d_slots, int nslots, int max_tiles, int it, int par,
+                                 cudaStream_t st) {
+    dim3 grid(max_tiles, nslots);
+    if (tc.tz == 32 && tc.tx == 32)
+        k_step<PSV, 32, 32><<<grid, kThreads, 0, st>>>(d_slots, it, par);
+    else if (tc.tz == 64 && tc.tx == 16)
+        k_step<PSV, 64, 16><<<grid, kThreads, 0, st>>>(d_slots, it, par);
+    else if (tc.tz == 32 && tc.tx == 16)
+        k_step<PSV, 32, 16><<<grid, kThreads, 0, st>>>(d_slots, it, par);
+    else if (tc.tz == 16 && tc.tx == 32)
+        k_step<PSV, 16, 32><<<grid, kThreads, 0, st>>>(d_slots, it, par);
+    else if (tc.tz == 128 && tc.tx == 8)
+        k_step<PSV, 128, 8><<<grid, kThreads, 0, st>>>(d_slots, it, par);
+    else
+        return cudaErrorInvalidValue;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_step(bool psv, TileCfg tc, const Slot *d_slots, int nslots, int max_tiles, int it, int par,
+                        cudaStream_t st) {
+    if (nslots <= 0 || max_tiles <= 0) return cudaSuccess;
+    return psv ? launch_step_t<true>(tc, d_slots, nslots, max_tiles, it, par, st)
+               : launch_step_t<false>(tc, d_slots, nslots, max_tiles, it, par, st);
+}
+
+// ------------------------------------------------------------ checkpoints
+// Forward checkpoints (solver/fdm.h:521-533,552-560): at the step with
+// (it+1) % sfe == 0, displacement is saved before the step and velocity after
+// it, into slot isfe = nsfe - (it+1)/sfe. Storage is FP32, BF16 or FP16; the
+// 16-bit forms use one power-of-two scale per snapshot and field, derived
+// from the field's max |value|, so the scaling itself adds no rounding.
+__device__ __forceinline__ float ckpt_scale(float amax, int prec) {
+    if (!(amax > 0.f) || prec == CKPT_F32) return 1.f;
+    // FP16: map amax to at most 2^15 (fp16 max 65504); BF16: to at most 1.
+    const float target = prec == CKPT_F16 ? 32768.f : 1.f;
+    int e;
+    frexpf(target / amax, &e);  // target/amax = m * 2^e, m in [0.5, 1)
+    return ldexpf(1.f, e - 1);  // largest power of two <= target/amax
+}
+
+// Fields of one checkpoint group: q index in the slot's checkpoint and the
+// state array that feeds it.
+__device__ __forceinline__ int ckpt_fields(const Slot &S, bool psv, int which_u, int par, const float **src,
+                                           int *q) {
+    const bool has_sh = S.sh[0] != nullptr;
+    if (!psv) {
+        src[0] = which_u ? S.sh[UY] : S.sh[VY0 + par];
+        q[0] = which_u ? 0 : 1;
+        return 1;
+    }
+    const int base = has_sh ? 2 : 0;
+    if (which_u) {
+        src[0] = S.psv[UX];
+        src[1] = S.psv[UZ];
+        q[0] = base + 0;
+        q[1] = base + 1;
+    } else {
+        src[0] = S.psv[VX0 + par];
+        src[1] = S.psv[VZ0 + par];
+        q[0] = base + 2;
+        q[1] = base + 3;
+    }
+    return 2;
+}
+
+__global__ void k_ckpt_amax(const Slot *__restrict__ slots, int isfe, int which_u, bool psv, int par) {
+    const Slot &S = slots[blockIdx.y];
+    if (!S.active || !S.ckpt || isfe < 0 || isfe >= S.nsfe) return;
+    if (psv ? S.psv[0] == nullptr : S.sh[0] == nullptr) return;
+    const float *src[2];
+    int q[2];
+    const int nfld = ckpt_fields(S, psv, which_u, par, src, q);
+    const size_t n = (size_t)S.nx * S.nz;
+    __shared__ float red[2][32];
+    for (int f = 0; f < nfld; f++) {
+        float m = 0.f;
+        for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+            m = fmaxf(m, fabsf(__ldg(src[f] + k)));
+        for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if ((threadIdx.x & 31) == 0) red[f][threadIdx.x >> 5] = m;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        for (int f = 0; f < nfld; f++) {
+            float m = threadIdx.x < (blockDim.x >> 5) ? red[f][threadIdx.x] : 0.f;
+            for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+            // non-negative floats order like their bit patterns
+            if (threadIdx.x == 0)
+                atomicMax(reinterpret_cast<unsigned *>(S.ckpt_amax) + (size_t)isfe * S.nf + q[f], __float_as_uint(m));
+        }
+    }
+}
+
+__global__ void k_ckpt_store(const Slot *__restrict__ slots, int isfe, int which_u, bool psv, int par) {
+    const Slot &S = slots[blockIdx.y];
+    if (!S.active || !S.ckpt || isfe < 0 || isfe >= S.nsfe) return;
+    if (psv ? S.psv[0] == nullptr : S.sh[0] == nullptr) return;
+    const float *src[2];
+    int q[2];
+    const int nfld = ckpt_fields(S, psv, which_u, par, src, q);
+    const size_t n = (size_t)S.nx * S.nz;
+    for (int f = 0; f < nfld; f++) {
+        const size_t off = ((size_t)isfe * S.nf + q[f]) * n;
+        if (S.ckpt_prec == CKPT_F32) {
+            float *dst = static_cast<float *>(S.ckpt) + off;
+            for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+                dst[k] = __ldg(src[f] + k);
+        } else {
+            const float sc = ckpt_scale(S.ckpt_amax[(size_t)isfe * S.nf + q[f]], S.ckpt_prec);
+            if (S.ckpt_prec == CKPT_BF16) {
+                __nv_bfloat16 *dst = static_cast<__nv_bfloat16 *>(S.ckpt) + off;
+                for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+                    dst[k] = __float2bfloat16_rn(__ldg(src[f] + k) * sc);
+            } else {
+                __half *dst = static_cast<__half *>(S.ckpt) + off;
+                for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+                    dst[k] = __float2half_rn(__ldg(src[f] + k) * sc);
+            }
+        }
+    }
+}
+
+static int ckpt_blocks(int n) {
+    int b = (n + 255) / 256;
+    return b < 1 ? 1 : (b > 1216 ? 1216 : b);
+}
+
+cudaError_t launch_ckpt_amax(const Slot *d_slots, int nslots, int n, int isfe, int which_u, bool psv, int par,
+                             cudaStream_t st) {
+    if (nslots <= 0) return cudaSuccess;
+    k_ckpt_amax<<<dim3(ckpt_blocks(n), nslots), 256, 0, st>>>(d_slots, isfe, which_u, psv, par);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ckpt_store(const Slot *d_slots, int nslots, int n, int isfe, int which_u, bool psv, int par,
+                              cudaStream_t st) {
+    if (nslots <= 0) return cudaSuccess;
+    k_ckpt_store<<<dim3(ckpt_blocks(n), nslots), 256, 0, st>>>(d_slots, isfe, which_u, psv, par);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ interaction
+// Sensitivity-kernel accumulation at adjoint steps with it % sfe == 0
+// (solver/fdm.h:583-606, interaction*: solver/fdm.h:198-219): gradients of the
+// adjoint displacement and of the checkpointed forward displacement, the
+// checkpointed forward velocity and the adjoint velocity, scaled by
+// ndt = sfe*dt. Each thread owns one cell and walks the group's slots in
+// order, so shots accumulate without atomics and deterministically.
+__device__ __forceinline__ float ck_load(const Slot &S, int isfe, int q, size_t k, size_t n, float inv) {
+    const size_t off = ((size_t)isfe * S.nf + q) * n + k;
+    if (S.ckpt_prec == CKPT_F32) return __ldg(static_cast<const float *>(S.ckpt) + off);
+    if (S.ckpt_prec == CKPT_BF16) return __bfloat162float(static_cast<const __nv_bfloat16 *>(S.ckpt)[off]) * inv;
+    return __half2float(static_cast<const __half *>(S.ckpt)[off]) * inv;
+}
+
+template <bool PSV>
+__global__ void k_interaction(const Slot *__restrict__ slots, const KernelGroup *__restrict__ groups, int isfe,
+                              float ndt, int par) {
+    const KernelGroup &G = groups[blockIdx.y];
+    const int nx = G.nx, nz = G.nz;
+    const size_t n = (size_t)nx * nz;
+    const size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int i = (int)(k / nz), j = (int)(k - (size_t)i * nz);
+    const bool gx = i >= 1 && i < nx - 2, gz = j >= 1 && j < nz - 2;
+    float kl = G.inv_lambda ? G.k_lambda[k] : 0.f;
+    float km = G.inv_mu ? G.k_mu[k] : 0.f;
+    float kr = G.inv_rho ? G.k_rho[k] : 0.f;
+    for (int s = G.first; s < G.first + G.count; s++) {
+        const Slot &S = slots[s];
+        if (!S.active || !S.ckpt) continue;
+        const float c9x = S.c9x, c24x = S.c24x, c9z = S.c9z, c24z = S.c24z;
+        const int base = (PSV && S.sh[0] != nullptr) ? 2 : 0;
+        const int nfu = PSV ? 2 : 1;
+        float inv[4];
+        for (int q = 0; q < 2 * nfu; q++) {
+            const float a = S.ckpt_amax ? S.ckpt_amax[(size_t)isfe * S.nf + base + q] : 0.f;
+            inv[q] = 1.f / ckpt_scale(a, S.ckpt_prec);
+        }
+        auto grad = [&](const float *w, float &ddx, float &ddz) {
+            ddx = gx ? dplus(__ldg(w + k + nz), __ldg(w + k), __ldg(w + k + 2 * nz), __ldg(w + k - nz), c9x, c24x) : 0.f;
+            ddz = gz ? dplus(__ldg(w + k + 1), __ldg(w + k), __ldg(w + k + 2), __ldg(w + k - 1), c9z, c24z) : 0.f;
+        };
+        auto grad_ck = [&](int q, float &ddx, float &ddz) {
+            const float iv = inv[q];
+            ddx = gx ? dplus(ck_load(S, isfe, base + q, k + nz, n, iv), ck_load(S, isfe, base + q, k, n, iv),
+                             ck_load(S, isfe, base + q, k + 2 * nz, n, iv), ck_load(S, isfe, base + q, k - nz, n, iv),
+                             c9x, c24x)
+                     : 0.f;
+            ddz = gz ? dplus(ck_load(S, isfe, base + q, k + 1, n, iv), ck_load(S, isfe, base + q, k, n, iv),
+                             ck_load(S, isfe, base + q, k + 2, n, iv), ck_load(S, isfe, base + q, k - 1, n, iv),
+                             c9z, c24z)
+                     : 0.f;
+        };
+        if (PSV) {
+            float dvxdx, dvxdz, dvzdx, dvzdz, fxdx, fxdz, fzdx, fzdz;
+            grad(S.psv[UX], dvxdx, dvxdz);
+            grad(S.psv[UZ], dvzdx, dvzdz);
+            grad_ck(0, fxdx, fxdz);
+            grad_ck(1, fzdx, fzdz);
+            if (G.inv_rho) {
+                const float vx_fw = ck_load(S, isfe, base + 2, k, n, inv[2]);
+                const float vz_fw = ck_load(S, isfe, base + 3, k, n, inv[3]);
+                kr -= (vx_fw * __ldg(S.psv[VX0 + par] + k) + vz_fw * __ldg(S.psv[VZ0 + par] + k)) * ndt;
+            }
+            if (G.inv_mu)
+                km -= (2.f * dvxdx * fxdx + 2.f * dvzdz * fzdz + (dvxdz + dvzdx) * (fzdx + fxdz)) * ndt;
+            if (G.inv_lambda) kl -= ((dvxdx + dvzdz) * (fxdx + fzdz)) * ndt;
+        } else {
+            float dvydx, dvydz, fdx, fdz;
+            grad(S.sh[UY], dvydx, dvydz);
+            grad_ck(0, fdx, fdz);
+            if (G.inv_rho) {
+                const float vy_fw = ck_load(S, isfe, 1, k, n, inv[1]);
+                kr -= vy_fw * __ldg(S.sh[VY0 + par] + k) * ndt;
+            }
+            if (G.inv_mu) km -= (dvydx * fdx + dvydz * fdz) * ndt;
+        }
+    }
+    if (G.inv_lambda) G.k_lambda[k] = kl;
+    if (G.inv_mu) G.k_mu[k] = km;
+    if (G.inv_rho) G.k_rho[k] = kr;
+}
+
+cudaError_t launch_interaction(bool psv, const Slot *d_slots, const KernelGroup *d_groups, int ngroups,
+                               int max_cells, int isfe, float ndt, int par, cudaStream_t st) {
+    if (ngroups <= 0) return cudaSuccess;
+    dim3 grid((max_cells + 255) / 256, ngroups);
+    if (psv)
+        k_interaction<true><<<grid, 256, 0, st>>>(d_slots, d_groups, isfe, ndt, par);
+    else
+        k_interaction<false><<<grid, 256, 0, st>>>(d_slots, d_groups, isfe, ndt, par);
+    return cudaGetLastError();
+}
+
+}  // namespace gb

@@ -1,0 +1,111 @@
+"""Seeded synthetic problems shared by the GPU parity tests, the smoke check
+and the benchmark's small cases.
+
+A case is a plain dict (grid, time axis, config values, sources, stations
+and the model on the grid). `gpu_solver` builds the library's solver from
+it through the C ABI; `oracle_problem` builds the CPU oracle's problem from
+the same numbers, so both sides see identical inputs.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+
+def layered_model(nx, nz, seed, vs_top=1700.0, vs_bottom=2300.0, nlayer=6, faults=1, jitter=0.03):
+    """vp, vs, rho (float32, reference layout k = i*nz + j) of a layered model
+    with dipping faults and a small random perturbation; vp = 1.73 vs,
+    rho = 310 vp^0.25 (Gardner)."""
+    rng = np.random.default_rng(seed)
+    ii, jj = np.meshgrid(np.arange(nx), np.arange(nz), indexing="ij")
+    depth = jj.astype(np.float64)
+    for _ in range(faults):
+        x0 = rng.uniform(0.2, 0.8) * nx
+        dip = rng.uniform(0.3, 1.0)
+        throw = rng.uniform(0.05, 0.15) * nz
+        depth = depth + np.where(ii + (jj - nz / 2) * dip > x0, throw, 0.0)
+    layer = np.clip((depth / nz * nlayer).astype(int), 0, nlayer - 1)
+    vs_l = np.linspace(vs_top, vs_bottom, nlayer)
+    vs = vs_l[layer] * (1 + jitter * rng.standard_normal((nx, nz)))
+    vp = 1.73 * vs
+    rho = 310.0 * vp ** 0.25
+    f = lambda a: np.ascontiguousarray(a.astype(np.float32).ravel())
+    return f(vp), f(vs), f(rho)
+
+
+def make_case(wave="psv", nx=120, nz=100, nt=600, nsrc=2, nrec=40, sfe=10, seed=0, dx=10.0, dt=1e-3,
+              f0=12.0, angle=math.pi / 4, amp=1e9, abs_width=12, model=None, both=False):
+    xmax = (nx - 1) * dx
+    zmax = (nz - 1) * dx
+    if model is None:
+        vp, vs, rho = layered_model(nx, nz, seed)
+    else:
+        vp, vs, rho = model
+    src = [[xmax * (0.2 + 0.6 * (s + 0.5) / nsrc), 3 * dx, 0, f0, 1.2 / f0, angle, amp] for s in range(nsrc)]
+    rec = [[xmax * (0.05 + 0.9 * r / max(nrec - 1, 1)), 2 * dx] for r in range(nrec)]
+    values = {
+        "mode": 2, "sh": int(wave == "sh" or both), "psv": int(wave == "psv" or both), "nt": nt, "dt": dt,
+        "sfe": sfe, "model_type": 0, "trace_type": 0,
+        "abs_left": 1, "abs_right": 1, "abs_bottom": 1, "abs_top": 0, "abs_width": abs_width,
+        "abs_alpha": 0.015, "inv_lambda": 1, "inv_mu": 1, "inv_rho": 1,
+    }
+    return dict(wave=wave, nx=nx, nz=nz, nt=nt, nsrc=nsrc, nrec=nrec, sfe=sfe, xmax=xmax, zmax=zmax,
+                values=values, src=src, rec=rec, vp=vp, vs=vs, rho=rho, dt=dt)
+
+
+def lame(orc, case):
+    """lambda, mu from vp, vs, rho with the oracle's vps2lm (float)."""
+    lam, mu = orc.vps2lm(case["vp"], case["vs"], case["rho"])
+    return lam, mu, case["rho"]
+
+
+def gpu_solver(pkg, case, directory=".", extra=None):
+    values = dict(case["values"])
+    values.update(extra or {})
+    cfg = pkg.Config.new(directory, values, case["src"], case["rec"])
+    sol = pkg.FdmSolver(cfg, grid=(case["nx"], case["nz"], case["xmax"], case["zmax"]))
+    vp, vs, rho = case["vp"], case["vs"], case["rho"]
+    # the same float arithmetic as vps2lm (solver/fdm.h:25-36)
+    lam = (rho * (vp * vp - np.float32(2) * vs * vs)).astype(np.float32)
+    lam = np.where(vp > vs, lam, np.float32(0)).astype(np.float32)
+    mu = (rho * vs * vs).astype(np.float32)
+    sol.set_model_grid(lam, mu, rho)
+    return cfg, sol
+
+
+def oracle_problem(orc, case, lam_mu_rho=None):
+    f32 = np.float32
+    nx, nz, nt = case["nx"], case["nz"], case["nt"]
+    xmax, zmax = f32(case["xmax"]), f32(case["zmax"])
+    dx = float(xmax / f32(nx - 1))
+    dz = float(zmax / f32(nz - 1))
+    v = case["values"]
+    if lam_mu_rho is None:
+        vp, vs, rho = case["vp"], case["vs"], case["rho"]
+        lam = (rho * (vp * vp - f32(2) * vs * vs)).astype(f32)
+        lam = np.where(vp > vs, lam, f32(0)).astype(f32)
+        mu = (rho * vs * vs).astype(f32)
+    else:
+        lam, mu, rho = lam_mu_rho
+    src = np.array(case["src"], f32).reshape(-1, 7)
+    rec = np.array(case["rec"], f32).reshape(-1, 2)
+    stf = [np.zeros(len(src) * nt, f32) for _ in range(3)]
+    for s in range(len(src)):
+        c = orc.ricker(nt, v["dt"], src[s, 3], src[s, 4], src[s, 5], src[s, 6])
+        for q in range(3):
+            stf[q][s * nt:(s + 1) * nt] = c[q]
+    ab = orc.absbound(nx, nz, v["abs_width"], v["abs_alpha"], v["abs_left"], v["abs_right"], v["abs_bottom"],
+                      v["abs_top"])
+    return orc.Problem(nx=nx, nz=nz, nt=nt, dx=dx, dz=dz, dt=float(f32(v["dt"])), sh=bool(v["sh"]),
+                       psv=bool(v["psv"]), sfe=v["sfe"], lam=lam, mu=mu, rho=rho, ab=ab, stf=tuple(stf),
+                       src_id=(orc.calc_idx(src[:, 0], float(xmax), nx), orc.calc_idx(src[:, 1], float(zmax), nz)),
+                       rec_id=(orc.calc_idx(rec[:, 0], float(xmax), nx), orc.calc_idx(rec[:, 1], float(zmax), nz)),
+                       inv_lambda=bool(v["inv_lambda"]), inv_mu=bool(v["inv_mu"]), inv_rho=bool(v["inv_rho"]))
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    den = np.linalg.norm(b)
+    return float(np.linalg.norm(a - b) / (den if den > 0 else 1.0))

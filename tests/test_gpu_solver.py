@@ -1,0 +1,138 @@
+"""GPU parity of the solver against the CPU oracle, through the C ABI.
+
+Tolerances: seismograms relative L2 <= 1e-5 after the full time loop;
+sensitivity kernels and misfits <= 1e-4 (FP32 arithmetic, the kernels
+replace divisions by reciprocal multiplies and contract into FMAs).
+Batching, tile shape and graph capture must not change any bit.
+"""
+import numpy as np
+import pytest
+
+from tests import cases
+
+pytestmark = pytest.mark.gpu
+
+TRACE_TOL = 1e-5
+KERNEL_TOL = 1e-4
+
+
+def comps(wave):
+    return "xz" if wave == "psv" else "y"
+
+
+def kernel_names(wave):
+    return ("k_lambda", "k_mu", "k_rho") if wave == "psv" else ("k_mu", "k_rho")
+
+
+@pytest.mark.parametrize("wave", ["psv", "sh"])
+def test_forward_traces_match_oracle(gpu, orc, wave):
+    case = cases.make_case(wave=wave, nx=150, nz=110, nt=700, nsrc=2, nrec=50, seed=3)
+    cfg, sol = cases.gpu_solver(gpu, case)
+    pb = cases.oracle_problem(orc, case)
+    for s in range(case["nsrc"]):
+        sol.runForward(s)
+        o = orc.forward(pb, s, adj=True)
+        for c in comps(wave):
+            assert cases.rel(sol.out(c), o["xyz".index(c)]) < TRACE_TOL
+
+
+@pytest.mark.parametrize("wave", ["psv", "sh"])
+def test_velocity_recording_without_adjoint(gpu, orc, wave):
+    # mode 3: no checkpoints, velocity recorded (trace_type 0)
+    case = cases.make_case(wave=wave, nx=90, nz=70, nt=400, nsrc=1, nrec=20, seed=5)
+    case["values"]["mode"] = 3
+    cfg, sol = cases.gpu_solver(gpu, case)
+    pb = cases.oracle_problem(orc, case)
+    sol.runForward(0)
+    o = orc.forward(pb, 0, adj=False, record_u=False)
+    for c in comps(wave):
+        assert cases.rel(sol.out(c), o["xyz".index(c)]) < TRACE_TOL
+
+
+def test_supershot_fires_every_source(gpu, orc):
+    case = cases.make_case(wave="psv", nx=100, nz=80, nt=400, nsrc=3, nrec=30, seed=9)
+    cfg, sol = cases.gpu_solver(gpu, case)
+    pb = cases.oracle_problem(orc, case)
+    sol.runForward(-1)
+    o = orc.forward(pb, -1, adj=True)
+    for c in "xz":
+        assert cases.rel(sol.out(c), o["xyz".index(c)]) < TRACE_TOL
+
+
+@pytest.mark.parametrize("wave", ["psv", "sh"])
+def test_adjoint_kernels_match_oracle(gpu, orc, wave):
+    case = cases.make_case(wave=wave, nx=120, nz=96, nt=500, nsrc=2, nrec=40, sfe=10, seed=11)
+    cfg, sol = cases.gpu_solver(gpu, case)
+    pb = cases.oracle_problem(orc, case)
+    rng = np.random.default_rng(2)
+    sol.initKernels()
+    kern = None
+    for s in range(case["nsrc"]):
+        sol.runForward(s)
+        o = orc.forward(pb, s, adj=True)
+        ad = {c: (rng.standard_normal((pb.nrec, pb.nt)) * 1e-3).astype(np.float32) for c in "xyz"}
+        for c in comps(wave):
+            sol.set_adstf(c, ad[c])
+        sol.runAdjoint(s)
+        kern = orc.adjoint(pb, [ad["x"], ad["y"], ad["z"]], o[3], kern)
+    k = sol.kernels()
+    for name in kernel_names(wave):
+        ref = kern[("k_lambda", "k_mu", "k_rho").index(name)]
+        assert cases.rel(k[name], ref) < KERNEL_TOL, name
+
+
+@pytest.mark.parametrize("wave", ["psv", "sh"])
+def test_batch_equals_one_shot_at_a_time(gpu, orc, wave):
+    case = cases.make_case(wave=wave, nx=110, nz=90, nt=300, nsrc=4, nrec=30, seed=13)
+    cfg, sol = cases.gpu_solver(gpu, case)
+    single = []
+    for s in range(4):
+        sol.runForward(s)
+        single.append({c: sol.out(c) for c in comps(wave)})
+    sol.run_forward_batch([0, 1, 2, 3])
+    for s in range(4):
+        for c in comps(wave):
+            np.testing.assert_array_equal(sol.out(c, slot=s), single[s][c])
+
+
+@pytest.mark.parametrize("tile", [1, 2, 3, 4, 5])
+def test_tile_shapes_give_identical_results(gpu, orc, tile):
+    case = cases.make_case(wave="psv", nx=133, nz=77, nt=250, nsrc=1, nrec=25, seed=17)
+    cfg, ref_sol = cases.gpu_solver(gpu, case)
+    ref_sol.set_option("tile", 1)
+    ref_sol.runForward(0)
+    ref = ref_sol.out("x"), ref_sol.out("z")
+    cfg2, sol = cases.gpu_solver(gpu, case)
+    sol.set_option("tile", tile)
+    sol.runForward(0)
+    np.testing.assert_array_equal(sol.out("x"), ref[0])
+    np.testing.assert_array_equal(sol.out("z"), ref[1])
+
+
+def test_graphs_and_eager_identical(gpu, orc):
+    case = cases.make_case(wave="sh", nx=100, nz=64, nt=300, nsrc=2, nrec=20, seed=19)
+    cfg, a = cases.gpu_solver(gpu, case)
+    a.set_option("graphs", 0)
+    cfg2, b = cases.gpu_solver(gpu, case)
+    b.set_option("graphs", 1)
+    for s in range(2):
+        a.runForward(s)
+        b.runForward(s)
+        np.testing.assert_array_equal(a.out("y"), b.out("y"))
+    rng = np.random.default_rng(0)
+    ad = (rng.standard_normal((case["nrec"], case["nt"])) * 1e-3).astype(np.float32)
+    for sol in (a, b):
+        sol.initKernels()
+        sol.set_adstf("y", ad)
+        sol.runAdjoint(1)
+    np.testing.assert_array_equal(a.kernels()["k_mu"], b.kernels()["k_mu"])
+
+
+def test_both_wave_systems_in_one_solver(gpu, orc):
+    case = cases.make_case(wave="psv", both=True, nx=90, nz=70, nt=300, nsrc=1, nrec=20, seed=23)
+    cfg, sol = cases.gpu_solver(gpu, case)
+    pb = cases.oracle_problem(orc, case)
+    sol.runForward(0)
+    o = orc.forward(pb, 0, adj=True)
+    for c in "xyz":
+        assert cases.rel(sol.out(c), o["xyz".index(c)]) < TRACE_TOL
