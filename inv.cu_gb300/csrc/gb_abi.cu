@@ -298,7 +298,7 @@ int gb_solver_set_option(gb_solver *s, const char *key, double value) {
         v.invalidate_graphs();
     } else if (k == "tile") {
         const int t = (int)value;
-        if (t < 0 || t > 5) return GB_ERR_ARG;
+        if (t < 0 || t > 20) return GB_ERR_ARG;
         v.opt_tile = t;
         if (t == 0) v.tile_id = 0;
         v.invalidate_graphs();

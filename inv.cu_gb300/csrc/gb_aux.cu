@@ -69,6 +69,20 @@ cudaError_t launch_mesh2grid(float *lambda, float *mu, float *rho, const float *
     return cudaGetLastError();
 }
 
+// out = 1/in rounded to nearest (the factor of dt*ds/rho in the velocity
+// update, solver/fdm.h:150-161); refreshed before each pass because the
+// model may change between passes.
+__global__ void k_reciprocal(float *out, const float *in, size_t n) {
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+        out[k] = __frcp_rn(in[k]);
+}
+
+cudaError_t launch_reciprocal(float *out, const float *in, size_t n, cudaStream_t st) {
+    if (!n) return cudaSuccess;
+    k_reciprocal<<<(unsigned)std::min<size_t>((n + 255) / 256, 4096), 256, 0, st>>>(out, in, n);
+    return cudaGetLastError();
+}
+
 // vps2lm (solver/fdm.h:25-36), in place.
 __global__ void k_vps2lm(float *lambda, float *mu, const float *rho, size_t n) {
     const size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;

@@ -31,6 +31,7 @@ struct Slot {
     float dt;
     float c9x, c24x, c9z, c24z;  // 9/(8h) and 1/(24h) for h = dx, dz
     const float *lambda, *mu, *rho;
+    const float *rinv;     // 1/rho rounded to nearest, refreshed at each pass
     const float *ax, *az;  // absorbing profiles: ab(i,j) = ax[i] * az[j]
     float *psv[NPSV];      // P-SV state (null when the slot has no P-SV)
     float *sh[NSH];        // SH state (null when the slot has no SH)
@@ -55,9 +56,11 @@ struct KernelGroup {
     int nx, nz;
 };
 
-// Tile configuration of the fused step kernel.
+// Configuration of the fused step kernel. threads == 0: 2-D tile kernel
+// owning tz x tx cells per block. threads > 0: marching kernel, one grid row
+// per thread, tz = threads - 6 owned rows per strip, tx = columns per chunk.
 struct TileCfg {
-    int tz, tx;
+    int tz, tx, threads;
 };
 
 // Packed tile CSR header: [0]=ntiles [1]=nentries [2]=ntraces, then
@@ -68,6 +71,8 @@ inline int csr_words(int ntiles, int nent, int ntr) { return 3 + ntiles + 1 + ne
 // All launchers enqueue on `st` and return cudaGetLastError().
 cudaError_t launch_step(bool psv, TileCfg tc, const Slot *d_slots, int nslots, int max_tiles, int it,
                         int par, cudaStream_t st);
+cudaError_t launch_march(bool psv, int threads, int chunk, const Slot *d_slots, int nslots, int max_tiles, int it,
+                         int par, cudaStream_t st);
 cudaError_t launch_ckpt_amax(const Slot *d_slots, int nslots, int n, int isfe, int which_u, bool psv,
                              int par, cudaStream_t st);
 cudaError_t launch_ckpt_store(const Slot *d_slots, int nslots, int n, int isfe, int which_u, bool psv,
@@ -80,6 +85,7 @@ cudaError_t launch_mesh2grid(float *lambda, float *mu, float *rho, const float *
                              float dz, int nx, int nz, cudaStream_t st);
 cudaError_t launch_scatter_points(float *lambda, float *mu, float *rho, const int *cell_of_point,
                                   const float *pa, const float *pb, const float *pr, int npt, cudaStream_t st);
+cudaError_t launch_reciprocal(float *out, const float *in, size_t n, cudaStream_t st);
 cudaError_t launch_vps2lm(float *lambda, float *mu, const float *rho, size_t n, cudaStream_t st);
 cudaError_t launch_lm2vps(float *vp, float *vs, const float *rho, size_t n, cudaStream_t st);
 cudaError_t launch_axpby(float *c, float ka, const float *a, float kb, const float *b, size_t n,

@@ -1,0 +1,381 @@
+// Marching step kernel: the production form of the fused time step.
+//
+// A block of T threads owns a z-strip (one grid row per thread) and marches
+// along x over a chunk of C columns. Window rows are [w0, w0 + T) with
+// w0 = strip * (T - 6) - 3; rows [w0 + 3, w0 + T - 3) are owned, the three
+// rows above and below are the halo the stencil needs. At column step p the
+// block
+//   * loads stress at column p (the x-neighbours of earlier columns stay in a
+//     4-deep register queue per thread),
+//   * computes the stress divergence and the new velocity and displacement at
+//     column p-1 (z-neighbours of stress come from shared memory, written at
+//     the previous step), adds the sources falling there, records receivers,
+//   * exchanges the new velocity of column p-1 through shared memory (the only
+//     barrier of the step; buffers are double-buffered by column parity),
+//   * updates stress at column p-3 from the velocity register queue
+//     (x-gradient) and the queued z-gradients.
+// Each field element is read once per step except the 3-column and 3-row
+// halos of a chunk, so the DRAM traffic stays near the algorithmic bytes and
+// the work per cell is a few dozen instructions. Loads for column p+1 are
+// issued before the arithmetic of column p.
+//
+// Arithmetic, guards and update order are those of the 2-D tile kernel
+// (solver/fdm.h:76-161): results do not depend on T, C or batching.
+#include "gb_internal.h"
+
+namespace gb {
+
+__device__ __forceinline__ float dminus_m(float a0, float am1, float ap1, float am2, float c9, float c24) {
+    return fmaf(a0 - am1, c9, -((ap1 - am2) * c24));
+}
+__device__ __forceinline__ float dplus_m(float ap1, float a0, float ap2, float am1, float c9, float c24) {
+    return fmaf(ap1 - a0, c9, -((ap2 - am1) * c24));
+}
+
+struct CsrM {
+    const int *tile_ptr, *local, *tptr, *traces;
+    __device__ CsrM(const int *p) {
+        const int ntiles = p[0], nent = p[1];
+        tile_ptr = p + 3;
+        local = tile_ptr + ntiles + 1;
+        tptr = local + nent;
+        traces = tptr + nent + 1;
+    }
+};
+
+constexpr int kMaxMarchThreads = 256;
+constexpr int kRing = 8;  // ring slots per thread: column p is read while p+1..p+7 are in flight
+
+// 4-byte async copy to shared address `d` (a 32-bit shared-window address);
+// pred == false zero-fills without reading (src stays a valid address).
+__device__ __forceinline__ void cpa4(unsigned d, const float *src, bool pred) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src), "r"(pred ? 4 : 0) : "memory");
+}
+__device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cpa_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// Words staged per column step: stress at p (NS), velocity, displacement and
+// reciprocal density at p-1 (2 NV + 1), the x-absorbing factor at p-1,
+// moduli at p-3.
+template <bool PSV>
+struct MarchWords {
+    static constexpr int NS = PSV ? 3 : 2, NV = PSV ? 2 : 1;
+    static constexpr int SG = 0, V = NS, U = NS + NV, RHO = NS + 2 * NV, AX = RHO + 1, MU = AX + 1,
+                         LAM = MU + 1, N = PSV ? LAM + 1 : MU + 1;
+};
+
+template <bool PSV>
+__host__ __device__ constexpr int march_smem_words(int threads) {
+    return (kRing * MarchWords<PSV>::N + 2 * ((PSV ? 2 : 1) + (PSV ? 2 : 1))) * threads + 2 * 2 * (2 + 2) * 2;
+}
+
+template <bool PSV>
+__global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restrict__ slots, int it, int par,
+                                                            int chunk) {
+    using W = MarchWords<PSV>;
+    constexpr int NS = W::NS, NV = W::NV;
+    constexpr int NZS = PSV ? 2 : 1;  // stress components with a z-derivative (sxz, szz | szy)
+    extern __shared__ float smem[];
+    const int T = blockDim.x, O = T - 6;
+    const int TP = T + 4;  // exchange rows padded by 2 on both sides
+    float *ring = smem;                                  // [kRing][W::N][T]
+    float *s_sz = ring + kRing * W::N * T;               // [2][NZS][TP]
+    float *s_vz = s_sz + 2 * NZS * TP;                   // [2][NV][TP]
+
+    const Slot &S = slots[blockIdx.y];
+    if (!S.active) return;
+    const int nx = S.nx, nz = S.nz, nt = S.nt;
+    const int tile = blockIdx.x;
+    if (tile >= S.tiles_z * S.tiles_x) return;
+    const int strip = tile % S.tiles_z, ck = tile / S.tiles_z;
+    const int t = threadIdx.x;
+    const int j = strip * O - 3 + t;          // grid row of this thread
+    const int c0 = ck * chunk;                 // first owned column
+    const int c1 = min(c0 + chunk, nx);        // one past the last owned column
+    const bool rowin = (unsigned)j < (unsigned)nz;
+    const bool rowown = t >= 3 && t < T - 3 && rowin;
+    const bool zS = j >= 2 && j < nz - 2;      // z part of the stress divergence
+    const bool zV = j >= 1 && j < nz - 2;      // z part of the velocity gradient
+    const float dt = S.dt, c9x = S.c9x, c24x = S.c24x, c9z = S.c9z, c24z = S.c24z;
+    const float azj = rowin ? __ldg(S.az + j) : 0.f;
+    const int st = t + 2;                      // padded exchange index
+    const int record_u = S.record_u;
+
+    const float *sig_in[NS];
+    float *sig_out[NS];
+    const float *v_in[NV];
+    float *v_out[NV];
+    float *u[NV];
+    if (PSV) {
+#pragma unroll
+        for (int f = 0; f < NS; f++) {
+            sig_in[f] = S.psv[SXX0 + 2 * f + par];
+            sig_out[f] = S.psv[SXX0 + 2 * f + (par ^ 1)];
+        }
+#pragma unroll
+        for (int f = 0; f < NV; f++) {
+            v_in[f] = S.psv[VX0 + 2 * f + par];
+            v_out[f] = S.psv[VX0 + 2 * f + (par ^ 1)];
+            u[f] = S.psv[UX + f];
+        }
+    } else {
+#pragma unroll
+        for (int f = 0; f < NS; f++) {
+            sig_in[f] = S.sh[SXY0 + 2 * f + par];
+            sig_out[f] = S.sh[SXY0 + 2 * f + (par ^ 1)];
+        }
+        v_in[0] = S.sh[VY0 + par];
+        v_out[0] = S.sh[VY0 + (par ^ 1)];
+        u[0] = S.sh[UY];
+    }
+    const float *lam = S.lambda, *mu = S.mu, *rinv_g = S.rinv, *ax = S.ax;
+
+    // Sources in the velocity region of this window and receivers of its
+    // owned cells, both sorted by column then row. The next entry's cell is
+    // kept in a register so the per-column test needs no memory access.
+    const int VZ = O + 3;
+    int inj_ptr = 0, inj_end = 0, rec_ptr = 0, rec_end = 0;
+    const int *inj_local = nullptr, *inj_tptr = nullptr, *inj_traces = nullptr;
+    const int *rec_local = nullptr, *rec_tptr = nullptr, *rec_traces = nullptr;
+    if (S.inj) {
+        const CsrM c(S.inj);
+        inj_ptr = c.tile_ptr[tile];
+        inj_end = c.tile_ptr[tile + 1];
+        inj_local = c.local;
+        inj_tptr = c.tptr;
+        inj_traces = c.traces;
+    }
+    if (S.rec) {
+        const CsrM c(S.rec);
+        rec_ptr = c.tile_ptr[tile];
+        rec_end = c.tile_ptr[tile + 1];
+        rec_local = c.local;
+        rec_tptr = c.tptr;
+        rec_traces = c.traces;
+    }
+    int inj_next = inj_ptr < inj_end ? inj_local[inj_ptr] : 0x7fffffff;
+    int rec_next = rec_ptr < rec_end ? rec_local[rec_ptr] : 0x7fffffff;
+
+    // Issues the loads of column step p into ring slot `slot` (own row only).
+    // Offsets are 32-bit (grids are limited to 2^29 cells); the shared
+    // address of this thread's ring row is computed once.
+    const unsigned ring_row = (unsigned)__cvta_generic_to_shared(ring + t);
+    const int jj = rowin ? j : 0;
+    auto issue = [&](int p, int slot) {
+        const unsigned rs = ring_row + (unsigned)(slot * W::N * T) * 4u;
+        const bool cs = (unsigned)p < (unsigned)nx && rowin;
+        const int ks = cs ? p * nz + jj : 0;
+#pragma unroll
+        for (int f = 0; f < NS; f++) cpa4(rs + (W::SG + f) * T * 4, sig_in[f] + ks, cs);
+        const int pv = p - 1;
+        const bool cv = (unsigned)pv < (unsigned)nx && rowin && pv >= c0 - 1;
+        const int kv = cv ? pv * nz + jj : 0;
+        const bool uo = cv && rowown && pv >= c0 && pv < c1;
+#pragma unroll
+        for (int f = 0; f < NV; f++) {
+            cpa4(rs + (W::V + f) * T * 4, v_in[f] + kv, cv);
+            cpa4(rs + (W::U + f) * T * 4, u[f] + kv, uo);
+        }
+        cpa4(rs + W::RHO * T * 4, rinv_g + kv, cv);
+        cpa4(rs + W::AX * T * 4, ax + (cv ? pv : 0), cv);
+        const int pm = p - 3;
+        const bool cm = pm >= c0 && pm < c1 && rowown;
+        const int km = cm ? pm * nz + jj : 0;
+        cpa4(rs + W::MU * T * 4, mu + km, cm);
+        if (PSV) cpa4(rs + W::LAM * T * 4, lam + km, cm);
+    };
+
+    float sq[4][NS], vq[4][NV], dzq[3][NV];
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+#pragma unroll
+        for (int f = 0; f < NS; f++) sq[a][f] = 0.f;
+#pragma unroll
+        for (int f = 0; f < NV; f++) vq[a][f] = 0.f;
+    }
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int f = 0; f < NV; f++) dzq[a][f] = 0.f;
+
+    const int p_first = c0 - 3, p_last = c1 + 2;
+    const int nstep = p_last - p_first + 1;
+    // prologue: kRing - 1 column steps in flight
+#pragma unroll
+    for (int q = 0; q < kRing - 1; q++) {
+        if (q < nstep) issue(p_first + q, q);
+        cpa_commit();
+    }
+    for (int q = 0; q < nstep; q++) {
+        const int p = p_first + q;
+        cpa_wait<kRing - 2>();  // column step q has landed (own row)
+        const float *rs = ring + (q % kRing) * W::N * T + t;
+        float cur[W::N];
+#pragma unroll
+        for (int w = 0; w < W::N; w++) cur[w] = rs[w * T];
+        // refill the slot read at the previous step
+        if (q + kRing - 1 < nstep) issue(p + kRing - 1, (q + kRing - 1) % kRing);
+        cpa_commit();
+
+        const int buf = q & 1;
+#pragma unroll
+        for (int f = 0; f < NS; f++) {
+            sq[0][f] = sq[1][f];
+            sq[1][f] = sq[2][f];
+            sq[2][f] = sq[3][f];
+            sq[3][f] = cur[W::SG + f];
+        }
+        float *sz_w = s_sz + buf * NZS * TP;
+        if (PSV) {
+            sz_w[st] = cur[W::SG + 2];       // sxz
+            sz_w[TP + st] = cur[W::SG + 1];  // szz
+        } else {
+            sz_w[st] = cur[W::SG + 1];  // szy
+        }
+        const int pv = p - 1;  // velocity column of this step
+        const bool vcol = pv >= c0 - 1;
+        float vn[NV];
+#pragma unroll
+        for (int f = 0; f < NV; f++) vn[f] = 0.f;
+        if (vcol) {
+            const float *sz_r = s_sz + (buf ^ 1) * NZS * TP;
+            float ds[NV];
+            const bool xS = pv >= 2 && pv < nx - 2;
+            if (PSV) {
+                float dsx = xS ? dminus_m(sq[2][0], sq[1][0], sq[3][0], sq[0][0], c9x, c24x) : 0.f;
+                float dsz = xS ? dminus_m(sq[2][2], sq[1][2], sq[3][2], sq[0][2], c9x, c24x) : 0.f;
+                if (zS) {
+                    const float *a = sz_r, *b = sz_r + TP;
+                    dsx += dminus_m(a[st], a[st - 1], a[st + 1], a[st - 2], c9z, c24z);
+                    dsz += dminus_m(b[st], b[st - 1], b[st + 1], b[st - 2], c9z, c24z);
+                }
+                ds[0] = dsx;
+                ds[NV - 1] = dsz;
+            } else {
+                float dsy = xS ? dminus_m(sq[2][0], sq[1][0], sq[3][0], sq[0][0], c9x, c24x) : 0.f;
+                if (zS) dsy += dminus_m(sz_r[st], sz_r[st - 1], sz_r[st + 1], sz_r[st - 2], c9z, c24z);
+                ds[0] = dsy;
+            }
+            // sources at this column, in trace order (solver/fdm.h:163-180)
+            const int cl = pv - (c0 - 1);
+            while (inj_next < (cl + 1) * VZ) {
+                if (t == inj_next - cl * VZ + 2) {
+                    for (int e = inj_tptr[inj_ptr]; e < inj_tptr[inj_ptr + 1]; e++) {
+                        const int ks = inj_traces[e] * nt + it;
+                        if (PSV) {
+                            ds[0] += __ldg(S.inj_x + ks);
+                            ds[NV - 1] += __ldg(S.inj_z + ks);
+                        } else {
+                            ds[0] += __ldg(S.inj_y + ks);
+                        }
+                    }
+                }
+                inj_ptr++;
+                inj_next = inj_ptr < inj_end ? inj_local[inj_ptr] : 0x7fffffff;
+            }
+            if ((unsigned)pv < (unsigned)nx && rowin) {
+                const float ab = cur[W::AX] * azj;
+                const float rinv = cur[W::RHO];
+#pragma unroll
+                for (int f = 0; f < NV; f++) vn[f] = ab * fmaf(dt * ds[f], rinv, cur[W::V + f]);
+            }
+            if (pv >= c0 && pv < c1) {
+                const int oc = pv - c0;
+                float un[NV];
+#pragma unroll
+                for (int f = 0; f < NV; f++) un[f] = cur[W::U + f] + vn[f] * dt;
+                if (rowown) {
+                    const int kv = pv * nz + j;
+#pragma unroll
+                    for (int f = 0; f < NV; f++) {
+                        v_out[f][kv] = vn[f];
+                        u[f][kv] = un[f];
+                    }
+                }
+                // receivers (solver/fdm.h:181-196): u when record_u, else v
+                while (rec_next < (oc + 1) * O) {
+                    if (rowown && t == rec_next - oc * O + 3) {
+                        for (int e = rec_tptr[rec_ptr]; e < rec_tptr[rec_ptr + 1]; e++) {
+                            const int kr = rec_traces[e] * nt + it;
+                            if (PSV) {
+                                S.out_x[kr] = record_u ? un[0] : vn[0];
+                                S.out_z[kr] = record_u ? un[NV - 1] : vn[NV - 1];
+                            } else {
+                                S.out_y[kr] = record_u ? un[0] : vn[0];
+                            }
+                        }
+                    }
+                    rec_ptr++;
+                    rec_next = rec_ptr < rec_end ? rec_local[rec_ptr] : 0x7fffffff;
+                }
+            }
+        }
+        float *vz_w = s_vz + buf * NV * TP;
+#pragma unroll
+        for (int f = 0; f < NV; f++) {
+            vq[0][f] = vq[1][f];
+            vq[1][f] = vq[2][f];
+            vq[2][f] = vq[3][f];
+            vq[3][f] = vn[f];
+            vz_w[f * TP + st] = vn[f];
+        }
+        __syncthreads();
+        // z-gradient of the new velocity at column pv
+#pragma unroll
+        for (int f = 0; f < NV; f++) {
+            dzq[0][f] = dzq[1][f];
+            dzq[1][f] = dzq[2][f];
+            const float *a = vz_w + f * TP;
+            dzq[2][f] = (vcol && zV) ? dplus_m(a[st + 1], a[st], a[st + 2], a[st - 1], c9z, c24z) : 0.f;
+        }
+        // stress update at column pm = p - 3 (solver/fdm.h:138-149)
+        const int pm = p - 3;
+        if (pm >= c0 && pm < c1 && rowown) {
+            const bool xV = pm >= 1 && pm < nx - 2;
+            const int km = pm * nz + j;
+            const float m = cur[W::MU];
+            if (PSV) {
+                const float dvxdx = xV ? dplus_m(vq[2][0], vq[1][0], vq[3][0], vq[0][0], c9x, c24x) : 0.f;
+                const float dvzdx = xV ? dplus_m(vq[2][1], vq[1][1], vq[3][1], vq[0][1], c9x, c24x) : 0.f;
+                const float dvxdz = dzq[0][0], dvzdz = dzq[0][1];
+                const float l = cur[W::LAM];
+                const float l2m = l + 2.f * m;
+                sig_out[0][km] = sq[0][0] + dt * (l2m * dvxdx + l * dvzdz);
+                sig_out[1][km] = sq[0][1] + dt * (l2m * dvzdz + l * dvxdx);
+                sig_out[2][km] = sq[0][2] + dt * (m * (dvxdz + dvzdx));
+            } else {
+                const float dvydx = xV ? dplus_m(vq[2][0], vq[1][0], vq[3][0], vq[0][0], c9x, c24x) : 0.f;
+                const float dvydz = dzq[0][0];
+                sig_out[0][km] = sq[0][0] + dt * m * dvydx;
+                sig_out[1][km] = sq[0][1] + dt * m * dvydz;
+            }
+        }
+    }
+    cpa_wait<0>();
+}
+
+cudaError_t launch_march(bool psv, int threads, int chunk, const Slot *d_slots, int nslots, int max_tiles, int it,
+                         int par, cudaStream_t st) {
+    if (nslots <= 0 || max_tiles <= 0) return cudaSuccess;
+    if (threads < 32 || threads > kMaxMarchThreads || threads % 32 || chunk < 1) return cudaErrorInvalidValue;
+    dim3 grid(max_tiles, nslots);
+    static bool attr_set[2] = {false, false};
+    const int maxw = psv ? march_smem_words<true>(kMaxMarchThreads) : march_smem_words<false>(kMaxMarchThreads);
+    if (!attr_set[psv]) {
+        cudaError_t e = psv ? cudaFuncSetAttribute(k_march<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxw * 4)
+                            : cudaFuncSetAttribute(k_march<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxw * 4);
+        if (e != cudaSuccess) return e;
+        attr_set[psv] = true;
+    }
+    const size_t smem = (size_t)(psv ? march_smem_words<true>(threads) : march_smem_words<false>(threads)) * 4;
+    if (psv)
+        k_march<true><<<grid, threads, smem, st>>>(d_slots, it, par, chunk);
+    else
+        k_march<false><<<grid, threads, smem, st>>>(d_slots, it, par, chunk);
+    return cudaGetLastError();
+}
+
+}  // namespace gb

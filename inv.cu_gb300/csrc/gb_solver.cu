@@ -20,8 +20,16 @@
 
 namespace gb {
 
-static const TileCfg kTiles[] = {{32, 32}, {32, 32}, {64, 16}, {32, 16}, {16, 32}, {128, 8}};
-static const int kNumTiles = 5;
+// Step-kernel configurations: ids 1-5 are 2-D tiles (rows x columns per
+// block), ids 6+ the marching kernel (threads per strip, columns per chunk).
+static const TileCfg kTiles[] = {
+    {32, 32, 0},                                                            // 0: unused
+    {32, 32, 0},   {64, 16, 0},   {32, 16, 0},   {16, 32, 0},   {128, 8, 0},  // 1-5
+    {58, 32, 64},  {90, 32, 96},  {122, 32, 128}, {122, 64, 128}, {154, 32, 160},  // 6-10
+    {154, 64, 160}, {186, 32, 192}, {250, 32, 256}, {250, 64, 256}, {122, 16, 128}, // 11-15
+    {58, 16, 64},  {250, 128, 256}, {122, 128, 128}, {154, 128, 160}, {154, 16, 160}, // 16-20
+};
+static const int kNumTiles = 20;
 
 // ---------------------------------------------------------------- tables
 // Packs a point set into the tile CSR the step kernel reads. For injection
@@ -210,6 +218,7 @@ int Solver::init(const Config &cfg, int nx_, int nz_, float xmax_, float zmax_) 
     GB_CUDA_TRY(cudaMalloc(&lambda, n * 4));
     GB_CUDA_TRY(cudaMalloc(&mu, n * 4));
     GB_CUDA_TRY(cudaMalloc(&rho, n * 4));
+    GB_CUDA_TRY(cudaMalloc(&rinv, n * 4));
     GB_CUDA_TRY(cudaMemset(lambda, 0, n * 4));
     GB_CUDA_TRY(cudaMemset(mu, 0, n * 4));
     GB_CUDA_TRY(cudaMemset(rho, 0, n * 4));
@@ -255,7 +264,7 @@ void Solver::release() {
         cudaFree(b.amax);
     }
     slots.clear();
-    for (float *p : {lambda, mu, rho, k_lambda, k_mu, k_rho, stf[0], stf[1], stf[2], ax, az}) cudaFree(p);
+    for (float *p : {lambda, mu, rho, rinv, k_lambda, k_mu, k_rho, stf[0], stf[1], stf[2], ax, az}) cudaFree(p);
     for (int q = 0; q < 3; q++) {
         cudaFree(d_slots[q]);
         cudaFreeHost(h_slots[q]);
@@ -488,6 +497,7 @@ int Solver::fill_slots(int kind, const int *shots, int n, bool record_u) {
         S.lambda = lambda;
         S.mu = mu;
         S.rho = rho;
+        S.rinv = rinv;
         S.ax = ax;
         S.az = az;
         float *p = B.state;
@@ -528,6 +538,17 @@ int Solver::fill_slots(int kind, const int *shots, int n, bool record_u) {
     return GB_OK;
 }
 
+// Records a timing event on st. Inside a stream capture a plain record only
+// marks a dependency; the external flag makes it a timestamped event node
+// (and is rejected outside a capture).
+cudaError_t Solver::record_timing(cudaEvent_t e) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaError_t err = cudaStreamIsCapturing(st, &cs);
+    if (err != cudaSuccess) return err;
+    return cs == cudaStreamCaptureStatusActive ? cudaEventRecordWithFlags(e, st, cudaEventRecordExternal)
+                                               : cudaEventRecord(e, st);
+}
+
 // Enqueues one pass on st (also used inside graph capture).
 int Solver::enqueue_pass(int kind, int n, bool snapshot, int snap_isrc) {
     const size_t nc = ncell();
@@ -561,11 +582,11 @@ int Solver::enqueue_pass(int kind, int n, bool snapshot, int snap_isrc) {
                 stats.launches += q16 ? 2 : 1;
             }
         }
-        if (it == w0 && win_steps > 0) GB_CUDA_TRY(cudaEventRecord(ev_win0, st));
+        if (it == w0 && win_steps > 0) GB_CUDA_TRY(record_timing(ev_win0));
         if (sh) GB_CUDA_TRY(launch_step(false, tile, ds, n, max_tiles(), it, par, st));
         if (psv) GB_CUDA_TRY(launch_step(true, tile, ds, n, max_tiles(), it, par, st));
         stats.launches += nwave;
-        if (it + 1 == w1 && win_steps > 0) GB_CUDA_TRY(cudaEventRecord(ev_win1, st));
+        if (it + 1 == w1 && win_steps > 0) GB_CUDA_TRY(record_timing(ev_win1));
         par ^= 1;
         if (isfe >= 0) {
             for (int w = 0; w < 2; w++) {
@@ -593,6 +614,7 @@ int Solver::enqueue_pass(int kind, int n, bool snapshot, int snap_isrc) {
 }
 
 int Solver::autotune(int n) {
+    GB_CUDA_TRY(launch_reciprocal(rinv, rho, ncell(), st));
     // Times every tile shape on the real batch (sources and receivers off,
     // results discarded) and keeps the fastest; the shape does not change
     // any computed value.
@@ -634,6 +656,7 @@ int Solver::autotune(int n) {
 
 int Solver::run_pass(int kind, int n, bool snapshot, int snap_isrc) {
     GB_CUDA_TRY(cudaEventRecord(ev_pass0, st));
+    GB_CUDA_TRY(launch_reciprocal(rinv, rho, ncell(), st));
     if (opt_graphs && !snapshot) {
         auto key = std::make_pair(kind, n);
         auto g = graphs.find(key);

@@ -62,6 +62,7 @@ struct Solver {
 
     // device buffers in the reference layout
     float *lambda = nullptr, *mu = nullptr, *rho = nullptr;
+    float *rinv = nullptr;  // 1/rho, refreshed at the start of every pass
     float *k_lambda = nullptr, *k_mu = nullptr, *k_rho = nullptr;
     float *stf[3] = {nullptr, nullptr, nullptr};
     float *ax = nullptr, *az = nullptr;
@@ -116,6 +117,7 @@ struct Solver {
     int export_snapshot(int it, int isrc, int par);
     int export_data(const std::string &comp, const float *d_data, int n);
     void invalidate_graphs();
+    cudaError_t record_timing(cudaEvent_t e);
     int max_tiles() const { return ((nz + tile.tz - 1) / tile.tz) * ((nx + tile.tx - 1) / tile.tx); }
 };
 

@@ -51,14 +51,33 @@ struct Csr {
     }
 };
 
+// Asynchronous 4-byte global->shared copy; with pred == false nothing is
+// read and the shared word is zero-filled (src must still be a valid address).
+__device__ __forceinline__ void cp_async4(float *dst, const float *src, bool pred) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    const int n = pred ? 4 : 0;
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src), "r"(n) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
+constexpr int kMaxInjTraces = 128;  // source samples staged in shared memory per tile
+
 template <bool PSV, int TZ, int TX>
 __global__ void __launch_bounds__(kThreads) k_step(const Slot *__restrict__ slots, int it, int par) {
     constexpr int NS = PSV ? 3 : 2;  // stress components held in shared memory
     constexpr int NV = PSV ? 2 : 1;  // velocity components
     constexpr int RZ = TZ + 6, RX = TX + 6;
     constexpr int VZ = TZ + 3, VX = TX + 3;
-    __shared__ float s_sig[NS][RX * RZ];
-    __shared__ float s_v[NV][VX * VZ];
+    constexpr int NR = RX * RZ, NVR = VX * VZ, NO = TX * TZ;
+    constexpr int QS = (NR + kThreads - 1) / kThreads;
+    constexpr int QV = (NVR + kThreads - 1) / kThreads;
+    constexpr int QO = (NO + kThreads - 1) / kThreads;
+    __shared__ float s_sig[NS][NR];
+    __shared__ float s_v[NV][NVR];  // velocity at time n, then n+1 (same cell, same thread)
+    __shared__ float s_rho[NVR];  // reciprocal density
+    __shared__ float s_inj[NV][kMaxInjTraces];
 
     const Slot &S = slots[blockIdx.y];
     if (!S.active) return;
@@ -67,6 +86,7 @@ __global__ void __launch_bounds__(kThreads) k_step(const Slot *__restrict__ slot
     if (tile >= S.tiles_z * S.tiles_x) return;
     const int tzi = tile % S.tiles_z, txi = tile / S.tiles_z;
     const int j0 = tzi * TZ, i0 = txi * TX;
+    const int tid = threadIdx.x;
 
     const float *sig_in[NS];
     float *sig_out[NS];
@@ -96,23 +116,106 @@ __global__ void __launch_bounds__(kThreads) k_step(const Slot *__restrict__ slot
         u[0] = S.sh[UY];
     }
     const float dt = S.dt, c9x = S.c9x, c24x = S.c24x, c9z = S.c9z, c24z = S.c24z;
+    const float *rho = S.rinv;  // reciprocal density, precomputed per pass
 
-    // 1. stress at time n on the tile + 3-cell halo (zero outside the grid;
-    //    those values only feed results the guards discard).
-    for (int e = threadIdx.x; e < RX * RZ; e += kThreads) {
-        const int c = e / RZ, r = e - c * RZ;
-        const int i = i0 - 3 + c, j = j0 - 3 + r;
-        const bool in = (unsigned)i < (unsigned)nx && (unsigned)j < (unsigned)nz;
-        const size_t k = (size_t)i * nz + j;
+    // ---- 0. issue every load of the tile before waiting for any.
+    // Stress at time n on the tile + 3-cell halo (zero outside the grid;
+    // those values only feed results the guards discard).
 #pragma unroll
-        for (int f = 0; f < NS; f++) s_sig[f][e] = in ? __ldg(sig_in[f] + k) : 0.f;
+    for (int q = 0; q < QS; q++) {
+        const int e = tid + q * kThreads;
+        if (e < NR) {
+            const int c = e / RZ, r = e - c * RZ;
+            const int i = i0 - 3 + c, j = j0 - 3 + r;
+            const bool in = (unsigned)i < (unsigned)nx && (unsigned)j < (unsigned)nz;
+            const size_t k = in ? (size_t)i * nz + j : 0;
+#pragma unroll
+            for (int f = 0; f < NS; f++) cp_async4(&s_sig[f][e], sig_in[f] + k, in);
+        }
     }
+    // Velocity at time n and density on the velocity region (tile + 1 cell
+    // before, 2 after).
+#pragma unroll
+    for (int q = 0; q < QV; q++) {
+        const int e = tid + q * kThreads;
+        if (e < NVR) {
+            const int c = e / VZ, r = e - c * VZ;
+            const int i = i0 - 1 + c, j = j0 - 1 + r;
+            const bool in = (unsigned)i < (unsigned)nx && (unsigned)j < (unsigned)nz;
+            const size_t k = in ? (size_t)i * nz + j : 0;
+#pragma unroll
+            for (int f = 0; f < NV; f++) cp_async4(&s_v[f][e], v_in[f] + k, in);
+            cp_async4(&s_rho[e], rho + k, in);
+        }
+    }
+    // Displacement of owned cells (velocity-region numbering) and the moduli
+    // of owned cells (tile numbering) go to registers.
+    float u_reg[QV][NV];
+#pragma unroll
+    for (int q = 0; q < QV; q++) {
+        const int e = tid + q * kThreads;
+        const int c = e / VZ, r = e - c * VZ;
+        const int i = i0 - 1 + c, j = j0 - 1 + r;
+        const bool own = e < NVR && c >= 1 && c <= TX && r >= 1 && r <= TZ && i < nx && j < nz;
+#pragma unroll
+        for (int f = 0; f < NV; f++) u_reg[q][f] = own ? u[f][(size_t)i * nz + j] : 0.f;
+    }
+    float mu_reg[QO], lam_reg[QO];
+#pragma unroll
+    for (int q = 0; q < QO; q++) {
+        const int e = tid + q * kThreads;
+        const int c = e / TZ, r = e - c * TZ;
+        const int i = i0 + c, j = j0 + r;
+        const bool in = e < NO && i < nx && j < nz;
+        const size_t k = in ? (size_t)i * nz + j : 0;
+        mu_reg[q] = in ? __ldg(S.mu + k) : 0.f;
+        lam_reg[q] = (PSV && in) ? __ldg(S.lambda + k) : 0.f;
+    }
+    // Source (or adjoint-source) samples falling in the velocity region.
+    int ninj = 0, inj_first = 0, tr_first = 0, ntr = 0;
+    const int *inj_local = nullptr, *inj_tptr = nullptr;
+    if (S.inj) {
+        const Csr cs(S.inj);
+        inj_first = cs.tile_ptr[tile];
+        ninj = cs.tile_ptr[tile + 1] - inj_first;
+        if (ninj) {
+            inj_local = cs.local;
+            inj_tptr = cs.tptr;
+            tr_first = cs.tptr[inj_first];
+            ntr = cs.tptr[inj_first + ninj] - tr_first;
+            if (ntr <= kMaxInjTraces) {
+                const int nt = S.nt;
+                for (int t = tid; t < ntr; t += kThreads) {
+                    const size_t ks = (size_t)cs.traces[tr_first + t] * nt + it;
+                    if (PSV) {
+                        s_inj[0][t] = __ldg(S.inj_x + ks);
+                        s_inj[NV - 1][t] = __ldg(S.inj_z + ks);
+                    } else {
+                        s_inj[0][t] = __ldg(S.inj_y + ks);
+                    }
+                }
+            }
+        }
+    }
+    cp_async_wait_all();
     __syncthreads();
 
-    // 2. stress divergence on the velocity region (tile + 1 before, 2 after).
-    auto divergence = [&](int c, int r, int i, int j, float *ds) {
+    // ---- 1. stress divergence, source samples (added in trace order,
+    //         solver/fdm.h:163-180), velocity and displacement updates.
+#pragma unroll
+    for (int q = 0; q < QV; q++) {
+        const int e = tid + q * kThreads;
+        if (e >= NVR) continue;
+        const int c = e / VZ, r = e - c * VZ;
+        const int i = i0 - 1 + c, j = j0 - 1 + r;
+        if (!((unsigned)i < (unsigned)nx && (unsigned)j < (unsigned)nz)) {
+#pragma unroll
+            for (int f = 0; f < NV; f++) s_v[f][e] = 0.f;
+            continue;
+        }
         const int cc = c + 2, rr = r + 2;
 #define SG(f, dc, dr) s_sig[f][(cc + (dc)) * RZ + rr + (dr)]
+        float ds[NV];
         if (PSV) {
             float dsx = 0.f, dsz = 0.f;
             if (i >= 2 && i < nx - 2) {
@@ -132,90 +235,49 @@ __global__ void __launch_bounds__(kThreads) k_step(const Slot *__restrict__ slot
             ds[0] = dsy;
         }
 #undef SG
-    };
-    auto update_v = [&](int c, int r, int i, int j, const float *ds) {
-        const int e = c * VZ + r;
-        if ((unsigned)i < (unsigned)nx && (unsigned)j < (unsigned)nz) {
-            const size_t k = (size_t)i * nz + j;
-            const float ab = __ldg(S.ax + i) * __ldg(S.az + j);
-            const float rinv = __frcp_rn(__ldg(S.rho + k));
-            const bool own = c >= 1 && c <= TX && r >= 1 && r <= TZ;
+        if (ninj) {
+            for (int p = 0; p < ninj; p++) {
+                if (inj_local[inj_first + p] != e) continue;
+                for (int t = inj_tptr[inj_first + p]; t < inj_tptr[inj_first + p + 1]; t++) {
+                    if (ntr <= kMaxInjTraces) {
 #pragma unroll
-            for (int f = 0; f < NV; f++) {
-                const float vn = ab * fmaf(dt * ds[f], rinv, __ldg(v_in[f] + k));
-                s_v[f][e] = vn;
-                if (own) {
-                    v_out[f][k] = vn;
-                    u[f][k] = u[f][k] + vn * dt;
+                        for (int f = 0; f < NV; f++) ds[f] += s_inj[f][t - tr_first];
+                    } else {
+                        const Csr cs(S.inj);
+                        const size_t ks = (size_t)cs.traces[t] * S.nt + it;
+                        if (PSV) {
+                            ds[0] += __ldg(S.inj_x + ks);
+                            ds[NV - 1] += __ldg(S.inj_z + ks);
+                        } else {
+                            ds[0] += __ldg(S.inj_y + ks);
+                        }
+                    }
                 }
             }
-        } else {
+        }
+        const size_t k = (size_t)i * nz + j;
+        const float ab = __ldg(S.ax + i) * __ldg(S.az + j);
+        const float rinv = s_rho[e];
+        const bool own = c >= 1 && c <= TX && r >= 1 && r <= TZ;
 #pragma unroll
-            for (int f = 0; f < NV; f++) s_v[f][e] = 0.f;
-        }
-    };
-
-    int ninj = 0, inj_first = 0;
-    if (S.inj) {
-        const Csr cs(S.inj);
-        inj_first = cs.tile_ptr[tile];
-        ninj = cs.tile_ptr[tile + 1] - inj_first;
-    }
-    if (ninj == 0) {
-        for (int e = threadIdx.x; e < VX * VZ; e += kThreads) {
-            const int c = e / VZ, r = e - c * VZ;
-            const int i = i0 - 1 + c, j = j0 - 1 + r;
-            float ds[NV];
-            divergence(c, r, i, j, ds);
-            update_v(c, r, i, j, ds);
-        }
-    } else {
-        // Sources in this region: divergence first, then the samples are
-        // added in trace order (solver/fdm.h:163-180), then velocity.
-        for (int e = threadIdx.x; e < VX * VZ; e += kThreads) {
-            const int c = e / VZ, r = e - c * VZ;
-            float ds[NV];
-            divergence(c, r, i0 - 1 + c, j0 - 1 + r, ds);
-#pragma unroll
-            for (int f = 0; f < NV; f++) s_v[f][e] = ds[f];
-        }
-        __syncthreads();
-        const Csr cs(S.inj);
-        const int nt = S.nt;
-        for (int q = threadIdx.x; q < ninj; q += kThreads) {
-            const int ent = inj_first + q;
-            const int e = cs.local[ent];
-            float a0 = s_v[0][e], a1 = s_v[NV - 1][e];
-            for (int t = cs.tptr[ent]; t < cs.tptr[ent + 1]; t++) {
-                const size_t ks = (size_t)cs.traces[t] * nt + it;
-                if (PSV) {
-                    a0 += __ldg(S.inj_x + ks);
-                    a1 += __ldg(S.inj_z + ks);
-                } else {
-                    a0 += __ldg(S.inj_y + ks);
-                }
+        for (int f = 0; f < NV; f++) {
+            const float vn = ab * fmaf(dt * ds[f], rinv, s_v[f][e]);
+            s_v[f][e] = vn;
+            if (own) {
+                v_out[f][k] = vn;
+                u[f][k] = u_reg[q][f] + vn * dt;
             }
-            s_v[0][e] = a0;
-            if (PSV) s_v[NV - 1][e] = a1;
-        }
-        __syncthreads();
-        for (int e = threadIdx.x; e < VX * VZ; e += kThreads) {
-            const int c = e / VZ, r = e - c * VZ;
-            float ds[NV];
-#pragma unroll
-            for (int f = 0; f < NV; f++) ds[f] = s_v[f][e];
-            update_v(c, r, i0 - 1 + c, j0 - 1 + r, ds);
         }
     }
     __syncthreads();
 
-    // 3. receivers owned by this tile (solver/fdm.h:181-196): u when
-    //    record_u (adjoint-capable runs or trace_type 1), else v.
+    // ---- 2. receivers owned by this tile (solver/fdm.h:181-196): u when
+    //         record_u (adjoint-capable runs or trace_type 1), else v.
     if (S.rec) {
         const Csr cs(S.rec);
         const int first = cs.tile_ptr[tile], nrec = cs.tile_ptr[tile + 1] - first;
         const int nt = S.nt;
-        for (int q = threadIdx.x; q < nrec; q += kThreads) {
+        for (int q = tid; q < nrec; q += kThreads) {
             const int ent = first + q;
             const int e = cs.local[ent];  // c * TZ + r within the owned tile
             const int c = e / TZ, r = e - c * TZ;
@@ -233,8 +295,11 @@ __global__ void __launch_bounds__(kThreads) k_step(const Slot *__restrict__ slot
         }
     }
 
-    // 4. stress update on owned cells (solver/fdm.h:138-149).
-    for (int e = threadIdx.x; e < TX * TZ; e += kThreads) {
+    // ---- 3. stress update on owned cells (solver/fdm.h:138-149).
+#pragma unroll
+    for (int q = 0; q < QO; q++) {
+        const int e = tid + q * kThreads;
+        if (e >= NO) continue;
         const int c = e / TZ, r = e - c * TZ;
         const int i = i0 + c, j = j0 + r;
         if (i >= nx || j >= nz) continue;
@@ -242,7 +307,7 @@ __global__ void __launch_bounds__(kThreads) k_step(const Slot *__restrict__ slot
         const int vc = c + 1, vr = r + 1;
         const int se = (c + 3) * RZ + (r + 3);
 #define VV(f, dc, dr) s_v[f][(vc + (dc)) * VZ + vr + (dr)]
-        const float m = __ldg(S.mu + k);
+        const float m = mu_reg[q];
         if (PSV) {
             float dvxdx = 0.f, dvzdx = 0.f, dvxdz = 0.f, dvzdz = 0.f;
             if (i >= 1 && i < nx - 2) {
@@ -253,7 +318,7 @@ __global__ void __launch_bounds__(kThreads) k_step(const Slot *__restrict__ slot
                 dvxdz = dplus(VV(0, 0, 1), VV(0, 0, 0), VV(0, 0, 2), VV(0, 0, -1), c9z, c24z);
                 dvzdz = dplus(VV(1, 0, 1), VV(1, 0, 0), VV(1, 0, 2), VV(1, 0, -1), c9z, c24z);
             }
-            const float l = __ldg(S.lambda + k);
+            const float l = lam_reg[q];
             const float l2m = l + 2.f * m;
             sig_out[0][k] = s_sig[0][se] + dt * (l2m * dvxdx + l * dvzdz);
             sig_out[1][k] = s_sig[1][se] + dt * (l2m * dvzdz + l * dvxdx);
@@ -291,6 +356,7 @@ static cudaError_t launch_step_t(TileCfg tc, const Slot *d_slots, int nslots, in
 cudaError_t launch_step(bool psv, TileCfg tc, const Slot *d_slots, int nslots, int max_tiles, int it, int par,
                         cudaStream_t st) {
     if (nslots <= 0 || max_tiles <= 0) return cudaSuccess;
+    if (tc.threads) return launch_march(psv, tc.threads, tc.tx, d_slots, nslots, max_tiles, it, par, st);
     return psv ? launch_step_t<true>(tc, d_slots, nslots, max_tiles, it, par, st)
                : launch_step_t<false>(tc, d_slots, nslots, max_tiles, it, par, st);
 }

@@ -95,18 +95,33 @@ def test_batch_equals_one_shot_at_a_time(gpu, orc, wave):
             np.testing.assert_array_equal(sol.out(c, slot=s), single[s][c])
 
 
-@pytest.mark.parametrize("tile", [1, 2, 3, 4, 5])
-def test_tile_shapes_give_identical_results(gpu, orc, tile):
-    case = cases.make_case(wave="psv", nx=133, nz=77, nt=250, nsrc=1, nrec=25, seed=17)
-    cfg, ref_sol = cases.gpu_solver(gpu, case)
-    ref_sol.set_option("tile", 1)
-    ref_sol.runForward(0)
-    ref = ref_sol.out("x"), ref_sol.out("z")
-    cfg2, sol = cases.gpu_solver(gpu, case)
-    sol.set_option("tile", tile)
-    sol.runForward(0)
-    np.testing.assert_array_equal(sol.out("x"), ref[0])
-    np.testing.assert_array_equal(sol.out("z"), ref[1])
+@pytest.mark.parametrize("wave", ["psv", "sh"])
+@pytest.mark.parametrize("tile", list(range(2, 21)))
+def test_kernel_configurations_give_identical_results(gpu, orc, tile, wave):
+    """2-D tiles (ids 1-5) and marching strips/chunks (ids 6-20) compute every
+    cell with the same operations in the same order."""
+    case = cases.make_case(wave=wave, nx=133, nz=77, nt=250, nsrc=2, nrec=25, seed=17)
+    rng = np.random.default_rng(5)
+    ad = {c: (rng.standard_normal((case["nrec"], case["nt"])) * 1e-3).astype(np.float32) for c in "xyz"}
+
+    def run(t):
+        cfg, sol = cases.gpu_solver(gpu, case)
+        sol.set_option("tile", t)
+        sol.run_forward_batch([0, 1])
+        tr = {c: sol.out(c, slot=1) for c in comps(wave)}
+        for c in comps(wave):
+            sol.set_adstf(c, ad[c], slot=0)
+            sol.set_adstf(c, ad[c], slot=1)
+        sol.initKernels()
+        sol.run_adjoint_batch([0, 1])
+        return tr, sol.kernels()
+
+    ref_tr, ref_k = run(1)
+    tr, k = run(tile)
+    for c in comps(wave):
+        np.testing.assert_array_equal(tr[c], ref_tr[c])
+    for name in kernel_names(wave):
+        np.testing.assert_array_equal(k[name], ref_k[name])
 
 
 def test_graphs_and_eager_identical(gpu, orc):
