@@ -91,6 +91,7 @@ def _declare(lib):
         "gb_filter_create": (_vp, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
         "gb_filter_apply": (ctypes.c_int, [_vp, _vp]),
         "gb_filter_destroy": (None, [_vp]),
+        "gb_filter_apply_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp]),
         "gb_misfit_create": (_vp, [_vp, _vp, _vp]),
         "gb_misfit_create_obs": (_vp, [ctypes.c_int, _vp, _vp, _fp, _fp, _fp]),
         "gb_misfit_set_obs": (ctypes.c_int, [_vp, _fp, _fp, _fp]),

@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 #include "gb_internal.h"
@@ -318,6 +319,83 @@ void gb_filter_destroy(gb_filter *f) {
     cudaFree(f->tmp);
     if (f->st) cudaStreamDestroy(f->st);
     delete f;
+}
+
+// ------------------------------------------------------------ C ABI: filter
+// without allocation (gb_filter_apply_noalloc)
+namespace {
+
+// Scratch of the allocation-free filter: the x-pass result and the weights
+// and partial-sum profiles. Reserved on every device that loads the library
+// for the life of the process (16 MiB + 96 KiB). Calls overwrite every
+// element they read, so nothing needs clearing between calls.
+static __device__ __align__(256) float g_na_tmp[GB_NOALLOC_MAX_CELLS];
+static __device__ __align__(256) float g_na_w[GB_NOALLOC_MAX_SIDE];
+static __device__ __align__(256) float g_na_sx[GB_NOALLOC_MAX_SIDE];
+static __device__ __align__(256) float g_na_sz[GB_NOALLOC_MAX_SIDE];
+
+// Device addresses of the arrays above, looked up once per device. In host
+// code the array names are host-side stand-ins, never device addresses.
+struct NoAllocAddr {
+    float *tmp = nullptr, *w = nullptr, *sx = nullptr, *sz = nullptr;
+    bool ready = false;
+};
+constexpr int kNoAllocDevices = 64;
+NoAllocAddr g_na_addr[kNoAllocDevices];
+std::mutex g_na_mutex;
+
+int noalloc_addresses(NoAllocAddr *out) {
+    int dev = 0;
+    GB_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocDevices) {
+        gb::set_error("gb_filter_apply_noalloc: device index out of range");
+        return GB_ERR_ARG;
+    }
+    std::lock_guard<std::mutex> lock(g_na_mutex);
+    NoAllocAddr &a = g_na_addr[dev];
+    if (!a.ready) {
+        GB_CUDA_TRY(cudaGetSymbolAddress((void **)&a.tmp, g_na_tmp));
+        GB_CUDA_TRY(cudaGetSymbolAddress((void **)&a.w, g_na_w));
+        GB_CUDA_TRY(cudaGetSymbolAddress((void **)&a.sx, g_na_sx));
+        GB_CUDA_TRY(cudaGetSymbolAddress((void **)&a.sz, g_na_sz));
+        a.ready = true;
+    }
+    *out = a;
+    return GB_OK;
+}
+
+}  // namespace
+
+extern "C" int gb_filter_apply_noalloc(int nx, int nz, int sigma, float *d_data) {
+    if (!d_data || nx < 1 || nz < 1 || sigma < 1) {
+        gb::set_error("gb_filter_apply_noalloc: need a device array and positive nx, nz, sigma");
+        return GB_ERR_ARG;
+    }
+    if ((long long)nx * nz > GB_NOALLOC_MAX_CELLS || std::max(nx, nz) > GB_NOALLOC_MAX_SIDE) {
+        gb::set_error("gb_filter_apply_noalloc: grid " + std::to_string(nx) + " x " + std::to_string(nz) +
+                      " exceeds the fixed scratch (at most " + std::to_string(GB_NOALLOC_MAX_CELLS) +
+                      " cells and " + std::to_string(GB_NOALLOC_MAX_SIDE) +
+                      " per side); use gb_filter_create / gb_filter_apply");
+        return GB_ERR_ARG;
+    }
+    NoAllocAddr a;
+    int rc = noalloc_addresses(&a);
+    if (rc) return rc;
+    const int len = std::max(nx, nz);
+    // Weights at distance >= 16 sigma are below 1e-55 and come out of expf
+    // as exactly 0, so summing from there (instead of from the last nonzero
+    // weight, which gb_filter_create reads back) adds only exact zeros.
+    const int m = std::min(len, (int)std::ceil(16.0 * sigma) + 2);
+    const size_t n = (size_t)nx * nz;
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    gb::k_gauss_weights<<<(len + 255) / 256, 256>>>(a.w, len, sigma);
+    gb::k_gauss_norm<<<(nx + 255) / 256, 256>>>(a.w, m, a.sx, nx);
+    gb::k_gauss_norm<<<(nz + 255) / 256, 256>>>(a.w, m, a.sz, nz);
+    gb::k_gauss_x<<<blocks, 256>>>(d_data, a.tmp, a.w, m, nx, nz);
+    gb::k_gauss_z<<<blocks, 256>>>(d_data, a.tmp, a.w, m, a.sx, a.sz, nx, nz);
+    GB_CUDA_TRY(cudaGetLastError());
+    GB_CUDA_TRY(cudaStreamSynchronize(0));
+    return GB_OK;
 }
 
 // ------------------------------------------------------------ C ABI: misc
