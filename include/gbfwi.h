@@ -188,7 +188,7 @@ int gb_filter_apply_noalloc(int nx, int nz, int sigma, float *d_data);
 typedef struct gb_misfit gb_misfit;
 /* Misfit::init (misfit/misfit.h:91-151): filter may be NULL (then one is made
  * from filter_sigma when filter == 0); observed traces are read from
- * traces/*.su when trace_file != 0, else generated on model_true; finally
+ * the traces/ SU files when trace_file != 0, else generated on model_true; finally
  * model_init is imported. */
 gb_misfit *gb_misfit_create(const gb_config *cfg, gb_solver *s, gb_filter *f);
 /* Same without files: observed traces from host arrays [nsrc][nrec][nt] per
@@ -216,6 +216,49 @@ int gb_optimizer_run(gb_optimizer *o);
 /* Misfit history of the last run: value of each accepted iteration. */
 int gb_optimizer_history(gb_optimizer *o, double *out, int n);
 void gb_optimizer_destroy(gb_optimizer *o);
+
+/* ----------------------------------------------------------------- Serving
+ * No counterpart in the reference, which solves one shot at a time; each
+ * request is the per-shot body of Misfit::run (misfit/misfit.h:29-44):
+ * forward with checkpoints, waveform misfit, adjoint with kernels. Requests
+ * have their own model, grid, step count and wave system; the engine admits
+ * them in arrival order while their device footprint fits the HBM budget,
+ * advances all admitted requests together (one launch per step), and frees
+ * each request's memory when its adjoint ends. A request's result does not
+ * depend on the other requests in flight. */
+typedef struct gb_server gb_server;
+typedef struct {
+    int psv;                  /* 1: P-SV, 0: SH */
+    int nx, nz;
+    float dx, dz, dt;
+    int nt;                   /* multiple of the server's sfe */
+    const float *lambda, *mu, *rho; /* host, nx*nz, reference layout; kept until the request ends */
+    float src[7];             /* x z type f0 t0 angle amp (one Ricker source) */
+    int nrec;
+    const float *rec;         /* host, nrec x (x, z) */
+    const float *obs;         /* host, [comp][nrec][nt] (x, z or y) or NULL for zeros */
+    int abs_width;
+    float abs_alpha;
+    int abs_left, abs_right, abs_bottom, abs_top;
+    int inv_lambda, inv_mu, inv_rho;
+    double arrival;           /* seconds after gb_server_run starts */
+} gb_request_desc;
+typedef struct {
+    int completed;
+    double wall_s, p50_s, p99_s; /* latency = completion - arrival */
+    int max_concurrent;
+    long long rounds, launches, cell_updates;
+} gb_server_stats;
+gb_server *gb_server_create(int sfe, int ckpt_precision, double hbm_budget_gb, int max_slots);
+/* Queues a request; returns its id (>= 0) or -1. */
+long long gb_server_submit(gb_server *srv, const gb_request_desc *req);
+/* Replays every queued request against the wall clock until all are done. */
+int gb_server_run(gb_server *srv);
+/* Kernels (host arrays of nx*nz, NULL to skip), misfit and latency. */
+int gb_server_result(gb_server *srv, long long id, float *k_lambda, float *k_mu, float *k_rho, double *misfit,
+                     double *latency_s);
+int gb_server_report(gb_server *srv, gb_server_stats *out);
+void gb_server_destroy(gb_server *srv);
 
 /* -------------------------------------------------------------- utilities */
 /* FP64 reductions over device float arrays (replace cublasSdot/Isamax/Snrm2

@@ -35,6 +35,24 @@ class GbError(RuntimeError):
     pass
 
 
+class RequestDesc(ctypes.Structure):
+    _fields_ = [("psv", ctypes.c_int), ("nx", ctypes.c_int), ("nz", ctypes.c_int), ("dx", ctypes.c_float),
+                ("dz", ctypes.c_float), ("dt", ctypes.c_float), ("nt", ctypes.c_int),
+                ("lambda_", ctypes.POINTER(ctypes.c_float)), ("mu", ctypes.POINTER(ctypes.c_float)),
+                ("rho", ctypes.POINTER(ctypes.c_float)), ("src", ctypes.c_float * 7), ("nrec", ctypes.c_int),
+                ("rec", ctypes.POINTER(ctypes.c_float)), ("obs", ctypes.POINTER(ctypes.c_float)),
+                ("abs_width", ctypes.c_int), ("abs_alpha", ctypes.c_float), ("abs_left", ctypes.c_int),
+                ("abs_right", ctypes.c_int), ("abs_bottom", ctypes.c_int), ("abs_top", ctypes.c_int),
+                ("inv_lambda", ctypes.c_int), ("inv_mu", ctypes.c_int), ("inv_rho", ctypes.c_int),
+                ("arrival", ctypes.c_double)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("completed", ctypes.c_int), ("wall_s", ctypes.c_double), ("p50_s", ctypes.c_double),
+                ("p99_s", ctypes.c_double), ("max_concurrent", ctypes.c_int), ("rounds", ctypes.c_longlong),
+                ("launches", ctypes.c_longlong), ("cell_updates", ctypes.c_longlong)]
+
+
 class GbStats(ctypes.Structure):
     _fields_ = [("forward_ms", ctypes.c_double), ("adjoint_ms", ctypes.c_double),
                 ("misfit_ms", ctypes.c_double), ("filter_ms", ctypes.c_double),
@@ -114,6 +132,13 @@ def _declare(lib):
         "gb_host_free": (ctypes.c_int, [_vp]),
         "gb_device_select": (ctypes.c_int, [ctypes.c_int]),
         "gb_solver_timer": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
+        "gb_server_create": (_vp, [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int]),
+        "gb_server_submit": (ctypes.c_longlong, [_vp, ctypes.POINTER(RequestDesc)]),
+        "gb_server_run": (ctypes.c_int, [_vp]),
+        "gb_server_result": (ctypes.c_int, [_vp, ctypes.c_longlong, _fp, _fp, _fp, ctypes.POINTER(ctypes.c_double),
+                                            ctypes.POINTER(ctypes.c_double)]),
+        "gb_server_report": (ctypes.c_int, [_vp, ctypes.POINTER(ServerStats)]),
+        "gb_server_destroy": (None, [_vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -499,6 +524,62 @@ class Optimizer:
     def close(self):
         if getattr(self, "_h", None) and _lib is not None:
             _lib.gb_optimizer_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+class Server:
+    """Continuous-batching engine for forward+adjoint shot requests."""
+
+    def __init__(self, sfe=10, ckpt=0, hbm_budget_gb=0.0, max_slots=0):
+        self._h = lib().gb_server_create(int(sfe), int(ckpt), float(hbm_budget_gb), int(max_slots))
+        if not self._h:
+            raise GbError(last_error())
+        self._keep = {}
+
+    def submit(self, *, psv, nx, nz, dx, dt, nt, lam, mu, rho, src, rec, obs=None, arrival=0.0, abs_width=20,
+               abs_alpha=0.015, abs_edges=(1, 1, 1, 0), inv=(1, 1, 1), dz=None) -> int:
+        arrs = [_f32(a).ravel() for a in (lam, mu, rho)]
+        recs = _f32(rec).ravel()
+        ob = _f32(obs).ravel() if obs is not None else None
+        d = RequestDesc()
+        d.psv, d.nx, d.nz, d.dx, d.dz, d.dt, d.nt = int(psv), nx, nz, dx, dz if dz else dx, dt, nt
+        d.lambda_, d.mu, d.rho = (_ptr(a) for a in arrs)
+        d.src = (ctypes.c_float * 7)(*src)
+        d.nrec = recs.size // 2
+        d.rec = _ptr(recs)
+        d.obs = _ptr(ob) if ob is not None else None
+        d.abs_width, d.abs_alpha = abs_width, abs_alpha
+        d.abs_left, d.abs_right, d.abs_bottom, d.abs_top = abs_edges
+        d.inv_lambda, d.inv_mu, d.inv_rho = inv
+        d.arrival = arrival
+        rid = lib().gb_server_submit(self._h, ctypes.byref(d))
+        if rid < 0:
+            raise GbError(last_error())
+        self._keep[rid] = (arrs, recs, ob, nx * nz)
+        return rid
+
+    def run(self):
+        check(lib().gb_server_run(self._h), "server run")
+
+    def result(self, rid):
+        n = self._keep[rid][3]
+        ks = [np.zeros(n, np.float32) for _ in range(3)]
+        mis, lat = ctypes.c_double(), ctypes.c_double()
+        check(lib().gb_server_result(self._h, rid, *[_ptr(k) for k in ks], ctypes.byref(mis), ctypes.byref(lat)),
+              "server result")
+        return {"k_lambda": ks[0], "k_mu": ks[1], "k_rho": ks[2], "misfit": mis.value, "latency": lat.value}
+
+    def stats(self) -> ServerStats:
+        s = ServerStats()
+        check(lib().gb_server_report(self._h, ctypes.byref(s)))
+        return s
+
+    def close(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.gb_server_destroy(self._h)
             self._h = None
 
     def __del__(self):

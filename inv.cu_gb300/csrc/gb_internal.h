@@ -28,6 +28,13 @@ struct Slot {
     int nx, nz, nt;
     int tiles_z, tiles_x;
     int active;
+    // Time base: a launch with step index k advances this slot from step
+    // it = it_base + k, reading the ping-pong buffers of parity
+    // (par0 + k) & 1. Lockstep batches use it_base = par0 = 0 and k = it;
+    // served requests each keep their own base.
+    int it_base, par0;
+    int sfe;         // checkpoint spacing (steps)
+    int ckpt_write;  // 1: forward pass stores checkpoints; 0: adjoint reads them
     float dt;
     float c9x, c24x, c9z, c24z;  // 9/(8h) and 1/(24h) for h = dx, dz
     const float *lambda, *mu, *rho;
@@ -69,16 +76,21 @@ inline int csr_words(int ntiles, int nent, int ntr) { return 3 + ntiles + 1 + ne
 
 // ---------------------------------------------------------------- launchers
 // All launchers enqueue on `st` and return cudaGetLastError().
-cudaError_t launch_step(bool psv, TileCfg tc, const Slot *d_slots, int nslots, int max_tiles, int it,
-                        int par, cudaStream_t st);
-cudaError_t launch_march(bool psv, int threads, int chunk, const Slot *d_slots, int nslots, int max_tiles, int it,
-                         int par, cudaStream_t st);
-cudaError_t launch_ckpt_amax(const Slot *d_slots, int nslots, int n, int isfe, int which_u, bool psv,
-                             int par, cudaStream_t st);
-cudaError_t launch_ckpt_store(const Slot *d_slots, int nslots, int n, int isfe, int which_u, bool psv,
-                              int par, cudaStream_t st);
+// k is the launch's step index (see Slot::it_base).
+cudaError_t launch_step(bool psv, TileCfg tc, const Slot *d_slots, int nslots, int max_tiles, int k,
+                        cudaStream_t st);
+cudaError_t launch_march(bool psv, int threads, int chunk, const Slot *d_slots, int nslots, int max_tiles, int k,
+                         cudaStream_t st);
+// Checkpoint of displacement before step k (which_u = 1) or velocity after
+// it (which_u = 0), for every slot with ckpt_write whose step is a
+// checkpoint step ((it + 1) % sfe == 0).
+cudaError_t launch_ckpt_amax(const Slot *d_slots, int nslots, int n, int k, int which_u, bool psv,
+                             cudaStream_t st);
+cudaError_t launch_ckpt_store(const Slot *d_slots, int nslots, int n, int k, int which_u, bool psv,
+                              cudaStream_t st);
+// Kernel accumulation after step k for every group slot with it % sfe == 0.
 cudaError_t launch_interaction(bool psv, const Slot *d_slots, const KernelGroup *d_groups, int ngroups,
-                               int max_cells, int isfe, float ndt, int par, cudaStream_t st);
+                               int max_cells, int k, cudaStream_t st);
 cudaError_t launch_fill(float *p, float v, size_t n, cudaStream_t st);
 cudaError_t launch_mesh2grid(float *lambda, float *mu, float *rho, const float *px, const float *pz,
                              const float *pa, const float *pb, const float *pr, int npt, float dmax, float dx,

@@ -73,7 +73,7 @@ __host__ __device__ constexpr int march_smem_words(int threads) {
 }
 
 template <bool PSV>
-__global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restrict__ slots, int it, int par,
+__global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restrict__ slots, int kstep,
                                                             int chunk) {
     using W = MarchWords<PSV>;
     constexpr int NS = W::NS, NV = W::NV;
@@ -87,6 +87,9 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
 
     const Slot &S = slots[blockIdx.y];
     if (!S.active) return;
+    const int it = S.it_base + kstep;
+    if (it < 0 || it >= S.nt) return;
+    const int par = (S.par0 + kstep) & 1;
     const int nx = S.nx, nz = S.nz, nt = S.nt;
     const int tile = blockIdx.x;
     if (tile >= S.tiles_z * S.tiles_x) return;
@@ -357,8 +360,8 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
     cpa_wait<0>();
 }
 
-cudaError_t launch_march(bool psv, int threads, int chunk, const Slot *d_slots, int nslots, int max_tiles, int it,
-                         int par, cudaStream_t st) {
+cudaError_t launch_march(bool psv, int threads, int chunk, const Slot *d_slots, int nslots, int max_tiles, int k,
+                         cudaStream_t st) {
     if (nslots <= 0 || max_tiles <= 0) return cudaSuccess;
     if (threads < 32 || threads > kMaxMarchThreads || threads % 32 || chunk < 1) return cudaErrorInvalidValue;
     dim3 grid(max_tiles, nslots);
@@ -372,9 +375,9 @@ cudaError_t launch_march(bool psv, int threads, int chunk, const Slot *d_slots, 
     }
     const size_t smem = (size_t)(psv ? march_smem_words<true>(threads) : march_smem_words<false>(threads)) * 4;
     if (psv)
-        k_march<true><<<grid, threads, smem, st>>>(d_slots, it, par, chunk);
+        k_march<true><<<grid, threads, smem, st>>>(d_slots, k, chunk);
     else
-        k_march<false><<<grid, threads, smem, st>>>(d_slots, it, par, chunk);
+        k_march<false><<<grid, threads, smem, st>>>(d_slots, k, chunk);
     return cudaGetLastError();
 }
 

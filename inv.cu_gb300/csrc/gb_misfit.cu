@@ -90,6 +90,15 @@ __global__ void k_waveform(const TraceRef *__restrict__ tr, const float *__restr
     if (threadIdx.x == 0) val[blockIdx.x] = sqrt(acc) * (double)sqrt_dt;
 }
 
+// Waveform misfit over an arbitrary table of trace references (used by the
+// serving engine, one request at a time).
+cudaError_t launch_waveform_refs(const void *refs, const float *tw, int ntr, int nt, float sqrt_dt, double *val,
+                                 cudaStream_t st) {
+    if (ntr <= 0) return cudaSuccess;
+    k_waveform<<<ntr, 256, 0, st>>>(static_cast<const TraceRef *>(refs), tw, nt, sqrt_dt, val);
+    return cudaGetLastError();
+}
+
 // ---- envelope (misfit/envelope.h:4-90)
 // Rows of n complex samples; row < nrow_a come from `a` rows, the rest from
 // `b` rows (real part, imaginary 0).

@@ -1,0 +1,652 @@
+// Serving engine: continuous batching of forward+adjoint shot requests.
+//
+// Each request is one shot on its own model and grid (its own nx, nz, nt,
+// wave system, sources and receivers): forward with checkpoints, waveform
+// misfit against its observed traces, adjoint with kernel accumulation. The
+// engine replays a stream of requests with arrival times. Before every round
+// it admits the requests that have arrived, in arrival order, while their
+// device footprint (model, wavefields, traces, checkpoints, kernels) fits the
+// HBM budget and a slot is free. A round advances every admitted request by
+// `sfe` steps: one step launch per wave system covers all of them, whatever
+// their grid size or phase (forward or adjoint), because every request keeps
+// its own time base in its slot descriptor. Requests that finish their
+// forward get their misfit and adjoint sources and start the adjoint in the
+// next round; requests that finish their adjoint return their kernels and
+// leave, freeing memory for waiting requests.
+//
+// Every request computes exactly the operations of a lone solve, in the
+// same order, so its result does not depend on what else is in flight.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <thread>
+#include <vector>
+
+#include "gb_solver.h"
+
+namespace gb {
+
+// kernels of gb_misfit.cu used per request
+cudaError_t launch_taper(float *tw, float dt, int nt, cudaStream_t st);
+struct TraceRefS {
+    const float *syn;
+    const float *obs;
+    float *adstf;
+};
+cudaError_t launch_waveform_refs(const void *refs, const float *tw, int ntr, int nt, float sqrt_dt, double *val,
+                                 cudaStream_t st);
+
+namespace {
+
+constexpr int kServerTile = 3;  // 2-D tiles 32 x 16: good across request sizes
+const TileCfg kSrvTile = {32, 16, 0};
+
+struct Req {
+    long long id = 0;
+    gb_request_desc d{};
+    // device block and views
+    char *blk = nullptr;
+    size_t bytes = 0;
+    float *lam = nullptr, *mu = nullptr, *rho = nullptr, *rinv = nullptr, *ax = nullptr, *az = nullptr;
+    float *stf = nullptr, *state = nullptr, *out[3] = {}, *adstf[3] = {}, *obs[3] = {}, *k[3] = {};
+    float *tw = nullptr, *amax = nullptr;
+    void *ckpt = nullptr;
+    double *val = nullptr;
+    TraceRefS *refs = nullptr;
+    int *csr_src = nullptr, *csr_rin = nullptr, *csr_rec = nullptr;
+    int nsfe = 0, nf = 0, ncomp = 0;
+    // progress
+    int phase = 0;  // 0 waiting, 1 forward, 2 adjoint, 3 done
+    int it = 0;
+    double t_admit = 0, t_done = 0;
+    double misfit = 0;
+    std::vector<float> res[3];
+};
+
+size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+}  // namespace
+
+struct Server {
+    int sfe = 10, prec = CKPT_F32, max_slots = 64;
+    double budget = 0;
+    size_t used = 0;
+    cudaStream_t st = nullptr;
+    std::vector<Req> reqs;
+    // Slot and group tables: one device copy, and a ring of pinned host
+    // staging buffers; a staging buffer is refilled only after the event
+    // recorded behind its previous copy has completed.
+    static constexpr int kStage = 4;
+    Slot *d_tab = nullptr, *h_tab[kStage] = {};
+    KernelGroup *d_grp = nullptr, *h_grp[kStage] = {};
+    cudaEvent_t copied[kStage] = {};
+    int tab_cap = 0;
+    // statistics
+    int max_active = 0;
+    long long rounds = 0, launches = 0;
+    double run_s = 0;
+
+    size_t footprint(const gb_request_desc &d, int nf, int nsfe, int ncomp) const {
+        const size_t n = (size_t)d.nx * d.nz;
+        const size_t tr = (size_t)d.nrec * d.nt;
+        const int nfield = d.psv ? NPSV : NSH;
+        size_t b = 0;
+        b += align256(4 * n * 4);                                  // lam mu rho rinv
+        b += align256((size_t)(d.nx + d.nz) * 4);                  // ax az
+        b += align256((size_t)3 * d.nt * 4);                       // stf
+        b += align256((size_t)nfield * n * 4);                     // state
+        b += 3 * align256((size_t)ncomp * tr * 4);                 // out, adstf, obs
+        b += align256(3 * n * 4);                                  // kernels
+        b += align256((size_t)d.nt * 4);                           // taper
+        b += align256((size_t)nsfe * nf * 4);                      // amax
+        b += align256((size_t)nsfe * nf * n * (prec == CKPT_F32 ? 4 : 2));
+        b += align256((size_t)ncomp * d.nrec * 8);                 // misfit values
+        b += align256((size_t)ncomp * d.nrec * sizeof(TraceRefS));
+        return b;
+    }
+};
+
+}  // namespace gb
+
+using namespace gb;
+
+struct gb_server {
+    gb::Server s;
+};
+
+namespace {
+
+std::vector<int> csr_for(int nx, int nz, const std::vector<int> &ii, const std::vector<int> &jj, bool inj) {
+    // same packing as the solver's tables (tile 32 x 16)
+    const int tz = kSrvTile.tz, tx = kSrvTile.tx;
+    const int tiles_z = (nz + tz - 1) / tz, tiles_x = (nx + tx - 1) / tx, ntiles = tiles_z * tiles_x;
+    const int vz = tz + 3;
+    std::map<int, std::map<int, std::vector<int>>> per;
+    for (size_t q = 0; q < ii.size(); q++) {
+        const int i = ii[q], j = jj[q];
+        if (i < 0 || i >= nx || j < 0 || j >= nz) continue;
+        if (inj) {
+            for (int txi = std::max(0, (i - tx - 1) / tx - 1); txi <= std::min(tiles_x - 1, (i + 1) / tx); txi++) {
+                const int i0 = txi * tx;
+                if (i < i0 - 1 || i > i0 + tx + 1) continue;
+                for (int tzi = std::max(0, (j - tz - 1) / tz - 1); tzi <= std::min(tiles_z - 1, (j + 1) / tz); tzi++) {
+                    const int j0 = tzi * tz;
+                    if (j < j0 - 1 || j > j0 + tz + 1) continue;
+                    per[txi * tiles_z + tzi][(i - (i0 - 1)) * vz + (j - (j0 - 1))].push_back((int)q);
+                }
+            }
+        } else {
+            const int txi = i / tx, tzi = j / tz;
+            per[txi * tiles_z + tzi][(i - txi * tx) * tz + (j - tzi * tz)].push_back((int)q);
+        }
+    }
+    int nent = 0, ntr = 0;
+    for (auto &t : per) {
+        nent += (int)t.second.size();
+        for (auto &e : t.second) ntr += (int)e.second.size();
+    }
+    std::vector<int> out(csr_words(ntiles, nent, ntr));
+    out[0] = ntiles;
+    out[1] = nent;
+    out[2] = ntr;
+    int *tile_ptr = out.data() + 3, *local = tile_ptr + ntiles + 1, *tptr = local + nent, *traces = tptr + nent + 1;
+    int e = 0, t = 0;
+    auto itp = per.begin();
+    for (int tile = 0; tile < ntiles; tile++) {
+        tile_ptr[tile] = e;
+        if (itp != per.end() && itp->first == tile) {
+            for (auto &ent : itp->second) {
+                local[e] = ent.first;
+                tptr[e] = t;
+                for (int v : ent.second) traces[t++] = v;
+                e++;
+            }
+            ++itp;
+        }
+    }
+    tile_ptr[ntiles] = e;
+    tptr[nent] = t;
+    return out;
+}
+
+int calc_idx(float c, float L, int n) { return (int)((double)(c / L * (float)(n - 1)) + 0.5); }
+
+void ricker1(int nt, float dt, const float *cfg, float *sx, float *sy, float *sz) {
+    const float pi = 3.1415927f;
+    const float f0 = cfg[0], t0 = cfg[1], angle = cfg[2], amp = cfg[3];
+    std::vector<float> s(nt);
+    float amax = 0;
+    for (int it = 0; it < nt; it++) {
+        float t = (float)(size_t)it * dt - t0;
+        float pft = pi * f0 * t;
+        s[it] = -t * expf(-pft * pft);
+        if (fabsf(s[it]) > amax) amax = fabsf(s[it]);
+    }
+    if (amax > 0)
+        for (int it = 0; it < nt; it++) s[it] /= amax;
+    for (int it = 0; it < nt; it++) {
+        sx[it] = amp * s[it] * cosf(angle);
+        sy[it] = amp * s[it];
+        sz[it] = amp * s[it] * sinf(angle);
+    }
+}
+
+// Uploads a request into its device block (model, profiles, source, obs,
+// tables) and zeroes state, kernels and checkpoint scales.
+int admit(Server &S, Req &r) {
+    const gb_request_desc &d = r.d;
+    const size_t n = (size_t)d.nx * d.nz, tr = (size_t)d.nrec * d.nt;
+    GB_CUDA_TRY(cudaMallocAsync((void **)&r.blk, r.bytes, S.st));
+    char *p = r.blk;
+    auto take = [&](size_t b) {
+        char *q = p;
+        p += align256(b);
+        return q;
+    };
+    r.lam = (float *)take(4 * n * 4);
+    r.mu = r.lam + n;
+    r.rho = r.lam + 2 * n;
+    r.rinv = r.lam + 3 * n;
+    r.ax = (float *)take((size_t)(d.nx + d.nz) * 4);
+    r.az = r.ax + d.nx;
+    r.stf = (float *)take((size_t)3 * d.nt * 4);
+    const int nfield = d.psv ? NPSV : NSH;
+    r.state = (float *)take((size_t)nfield * n * 4);
+    const int comps_psv[2] = {0, 2}, comps_sh[1] = {1};
+    const int *cs = d.psv ? comps_psv : comps_sh;
+    float *outb = (float *)take((size_t)r.ncomp * tr * 4);
+    float *adb = (float *)take((size_t)r.ncomp * tr * 4);
+    float *obb = (float *)take((size_t)r.ncomp * tr * 4);
+    for (int q = 0; q < r.ncomp; q++) {
+        r.out[cs[q]] = outb + q * tr;
+        r.adstf[cs[q]] = adb + q * tr;
+        r.obs[cs[q]] = obb + q * tr;
+    }
+    float *kb = (float *)take(3 * n * 4);
+    for (int q = 0; q < 3; q++) r.k[q] = kb + q * n;
+    r.tw = (float *)take((size_t)d.nt * 4);
+    r.amax = (float *)take((size_t)r.nsfe * r.nf * 4);
+    r.ckpt = take((size_t)r.nsfe * r.nf * n * (S.prec == CKPT_F32 ? 4 : 2));
+    r.val = (double *)take((size_t)r.ncomp * d.nrec * 8);
+    r.refs = (TraceRefS *)take((size_t)r.ncomp * d.nrec * sizeof(TraceRefS));
+
+    // host-side preparation
+    const float xmax = d.dx * (d.nx - 1), zmax = d.dz * (d.nz - 1);
+    std::vector<float> hax(d.nx, 1.f), haz(d.nz, 1.f);
+    const int w = d.abs_width;
+    const float a = d.abs_alpha;
+    for (int i = 0; i < d.nx; i++) {
+        if (d.abs_left && i + 1 < w) hax[i] *= expf(-powf(a * (float)(w - i - 1), 2));
+        if (d.abs_right && i > d.nx - w) hax[i] *= expf(-powf(a * (float)(w + i - d.nx), 2));
+    }
+    for (int j = 0; j < d.nz; j++) {
+        if (d.abs_bottom && j > d.nz - w) haz[j] *= expf(-powf(a * (float)(w + j - d.nz), 2));
+        if (d.abs_top && j + 1 < w) haz[j] *= expf(-powf(a * (float)(w - j - 1), 2));
+    }
+    std::vector<float> hstf(3 * (size_t)d.nt);
+    ricker1(d.nt, d.dt, d.src + 3, hstf.data(), hstf.data() + d.nt, hstf.data() + 2 * d.nt);
+    const std::vector<int> si = {calc_idx(d.src[0], xmax, d.nx)}, sj = {calc_idx(d.src[1], zmax, d.nz)};
+    std::vector<int> ri(d.nrec), rj(d.nrec);
+    for (int q = 0; q < d.nrec; q++) {
+        ri[q] = calc_idx(d.rec[2 * q], xmax, d.nx);
+        rj[q] = calc_idx(d.rec[2 * q + 1], zmax, d.nz);
+    }
+    const std::vector<int> c1 = csr_for(d.nx, d.nz, si, sj, true);
+    const std::vector<int> c2 = csr_for(d.nx, d.nz, ri, rj, true);
+    const std::vector<int> c3 = csr_for(d.nx, d.nz, ri, rj, false);
+    GB_CUDA_TRY(cudaMallocAsync((void **)&r.csr_src, (c1.size() + c2.size() + c3.size()) * 4, S.st));
+    r.csr_rin = r.csr_src + c1.size();
+    r.csr_rec = r.csr_rin + c2.size();
+
+    // uploads (pageable sources are staged by the runtime; they stay valid
+    // until the request completes, by the API contract)
+    GB_CUDA_TRY(cudaMemcpyAsync(r.lam, d.lambda, n * 4, cudaMemcpyHostToDevice, S.st));
+    GB_CUDA_TRY(cudaMemcpyAsync(r.mu, d.mu, n * 4, cudaMemcpyHostToDevice, S.st));
+    GB_CUDA_TRY(cudaMemcpyAsync(r.rho, d.rho, n * 4, cudaMemcpyHostToDevice, S.st));
+    GB_CUDA_TRY(launch_reciprocal(r.rinv, r.rho, n, S.st));
+    GB_CUDA_TRY(cudaMemcpyAsync(r.ax, hax.data(), d.nx * 4, cudaMemcpyHostToDevice, S.st));
+    GB_CUDA_TRY(cudaMemcpyAsync(r.az, haz.data(), d.nz * 4, cudaMemcpyHostToDevice, S.st));
+    GB_CUDA_TRY(cudaMemcpyAsync(r.stf, hstf.data(), hstf.size() * 4, cudaMemcpyHostToDevice, S.st));
+    GB_CUDA_TRY(cudaMemcpyAsync(r.csr_src, c1.data(), c1.size() * 4, cudaMemcpyHostToDevice, S.st));
+    GB_CUDA_TRY(cudaMemcpyAsync(r.csr_rin, c2.data(), c2.size() * 4, cudaMemcpyHostToDevice, S.st));
+    GB_CUDA_TRY(cudaMemcpyAsync(r.csr_rec, c3.data(), c3.size() * 4, cudaMemcpyHostToDevice, S.st));
+    if (d.obs)
+        GB_CUDA_TRY(cudaMemcpyAsync(obb, d.obs, (size_t)r.ncomp * tr * 4, cudaMemcpyHostToDevice, S.st));
+    else
+        GB_CUDA_TRY(cudaMemsetAsync(obb, 0, (size_t)r.ncomp * tr * 4, S.st));
+    GB_CUDA_TRY(cudaMemsetAsync(r.state, 0, (size_t)nfield * n * 4, S.st));
+    GB_CUDA_TRY(cudaMemsetAsync(kb, 0, 3 * n * 4, S.st));
+    GB_CUDA_TRY(cudaMemsetAsync(r.amax, 0, (size_t)r.nsfe * r.nf * 4, S.st));
+    GB_CUDA_TRY(cudaMemsetAsync(outb, 0, (size_t)r.ncomp * tr * 4, S.st));
+    GB_CUDA_TRY(launch_taper(r.tw, d.dt, d.nt, S.st));
+    std::vector<TraceRefS> refs((size_t)r.ncomp * d.nrec);
+    for (int ir = 0; ir < d.nrec; ir++)
+        for (int q = 0; q < r.ncomp; q++) {
+            const size_t off = (size_t)ir * d.nt;
+            refs[(size_t)ir * r.ncomp + q] = {outb + q * tr + off, obb + q * tr + off, adb + q * tr + off};
+        }
+    GB_CUDA_TRY(cudaMemcpyAsync(r.refs, refs.data(), refs.size() * sizeof(TraceRefS), cudaMemcpyHostToDevice, S.st));
+    // the host vectors above die at return: finish the copies now
+    GB_CUDA_TRY(cudaStreamSynchronize(S.st));
+    r.phase = 1;
+    r.it = 0;
+    S.used += r.bytes;
+    return GB_OK;
+}
+
+void fill_slot(const Server &S, const Req &r, Slot &s) {
+    memset(&s, 0, sizeof s);
+    const gb_request_desc &d = r.d;
+    s.nx = d.nx;
+    s.nz = d.nz;
+    s.nt = d.nt;
+    s.tiles_z = (d.nz + kSrvTile.tz - 1) / kSrvTile.tz;
+    s.tiles_x = (d.nx + kSrvTile.tx - 1) / kSrvTile.tx;
+    s.active = 1;
+    s.it_base = r.it;
+    s.par0 = r.it & 1;
+    s.sfe = S.sfe;
+    s.dt = d.dt;
+    s.c9x = 9.f / (8.f * d.dx);
+    s.c24x = 1.f / (24.f * d.dx);
+    s.c9z = 9.f / (8.f * d.dz);
+    s.c24z = 1.f / (24.f * d.dz);
+    s.lambda = r.lam;
+    s.mu = r.mu;
+    s.rho = r.rho;
+    s.rinv = r.rinv;
+    s.ax = r.ax;
+    s.az = r.az;
+    const size_t n = (size_t)d.nx * d.nz;
+    if (d.psv)
+        for (int f = 0; f < NPSV; f++) s.psv[f] = r.state + f * n;
+    else
+        for (int f = 0; f < NSH; f++) s.sh[f] = r.state + f * n;
+    s.nsfe = r.nsfe;
+    s.nf = r.nf;
+    s.ckpt_prec = S.prec;
+    s.ckpt = r.ckpt;
+    s.ckpt_amax = r.amax;
+    if (r.phase == 1) {
+        s.inj = r.csr_src;
+        s.inj_x = r.stf;
+        s.inj_y = r.stf + d.nt;
+        s.inj_z = r.stf + 2 * d.nt;
+        s.rec = r.csr_rec;
+        s.out_x = r.out[0];
+        s.out_y = r.out[1];
+        s.out_z = r.out[2];
+        s.record_u = 1;
+        s.ckpt_write = 1;
+    } else {
+        s.inj = r.csr_rin;
+        s.inj_x = r.adstf[0];
+        s.inj_y = r.adstf[1];
+        s.inj_z = r.adstf[2];
+        s.ckpt_write = 0;
+    }
+}
+
+double now_s(std::chrono::steady_clock::time_point t0) {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+// One round: every active request advances sfe steps.
+int round_once(Server &S, std::vector<Req *> &act) {
+    // table: [P-SV adjoint, P-SV forward, SH adjoint, SH forward]
+    std::vector<Req *> order;
+    int counts[2][2] = {{0, 0}, {0, 0}};  // [psv][phase-1]
+    for (int w = 1; w >= 0; w--)
+        for (int ph = 2; ph >= 1; ph--)
+            for (Req *r : act)
+                if (r->d.psv == w && r->phase == ph) {
+                    order.push_back(r);
+                    counts[w][ph - 1]++;
+                }
+    const int n = (int)order.size();
+    if (n > S.tab_cap) {
+        GB_CUDA_TRY(cudaStreamSynchronize(S.st));
+        cudaFree(S.d_tab);
+        cudaFree(S.d_grp);
+        for (int b = 0; b < Server::kStage; b++) {
+            cudaFreeHost(S.h_tab[b]);
+            cudaFreeHost(S.h_grp[b]);
+        }
+        S.tab_cap = std::max(n, 2 * S.tab_cap);
+        GB_CUDA_TRY(cudaMalloc(&S.d_tab, sizeof(Slot) * S.tab_cap));
+        GB_CUDA_TRY(cudaMalloc(&S.d_grp, sizeof(KernelGroup) * S.tab_cap));
+        for (int b = 0; b < Server::kStage; b++) {
+            GB_CUDA_TRY(cudaMallocHost(&S.h_tab[b], sizeof(Slot) * S.tab_cap));
+            GB_CUDA_TRY(cudaMallocHost(&S.h_grp[b], sizeof(KernelGroup) * S.tab_cap));
+        }
+    }
+    const int b = (int)(S.rounds % Server::kStage);
+    if (!S.copied[b]) GB_CUDA_TRY(cudaEventCreateWithFlags(&S.copied[b], cudaEventDisableTiming));
+    GB_CUDA_TRY(cudaEventSynchronize(S.copied[b]));  // its previous copy has been consumed
+    Slot *h_tab = S.h_tab[b];
+    KernelGroup *h_grp = S.h_grp[b];
+    int max_tiles[2] = {0, 0}, max_cells[2] = {0, 0};
+    size_t max_n_fwd[2] = {0, 0};
+    for (int q = 0; q < n; q++) {
+        fill_slot(S, *order[q], h_tab[q]);
+        const int w = order[q]->d.psv;
+        max_tiles[w] = std::max(max_tiles[w], h_tab[q].tiles_z * h_tab[q].tiles_x);
+        const size_t cells = (size_t)order[q]->d.nx * order[q]->d.nz;
+        if (order[q]->phase == 2) max_cells[w] = std::max(max_cells[w], (int)cells);
+        if (order[q]->phase == 1) max_n_fwd[w] = std::max(max_n_fwd[w], cells);
+        KernelGroup &g = h_grp[q];
+        g.k_lambda = order[q]->k[0];
+        g.k_mu = order[q]->k[1];
+        g.k_rho = order[q]->k[2];
+        g.inv_lambda = order[q]->d.inv_lambda;
+        g.inv_mu = order[q]->d.inv_mu;
+        g.inv_rho = order[q]->d.inv_rho;
+        g.first = q;
+        g.count = 1;
+        g.nx = order[q]->d.nx;
+        g.nz = order[q]->d.nz;
+    }
+    GB_CUDA_TRY(cudaMemcpyAsync(S.d_tab, h_tab, sizeof(Slot) * n, cudaMemcpyHostToDevice, S.st));
+    GB_CUDA_TRY(cudaMemcpyAsync(S.d_grp, h_grp, sizeof(KernelGroup) * n, cudaMemcpyHostToDevice, S.st));
+    GB_CUDA_TRY(cudaEventRecord(S.copied[b], S.st));
+    const int base_psv = 0, n_psv = counts[1][0] + counts[1][1];
+    const int base_sh = n_psv, n_sh = counts[0][0] + counts[0][1];
+    const bool q16 = S.prec != CKPT_F32;
+    for (int k = 0; k < S.sfe; k++) {
+        for (int w = 1; w >= 0; w--) {
+            const int base = w ? base_psv : base_sh, cnt = w ? n_psv : n_sh;
+            if (!cnt) continue;
+            const int nadj = counts[w][1];
+            const Slot *tab = S.d_tab + base;
+            // forward checkpoints of u before the step (the kernels select
+            // the forward slots whose step is a checkpoint step)
+            if (k == S.sfe - 1 && cnt > nadj) {
+                if (q16) GB_CUDA_TRY(launch_ckpt_amax(tab, cnt, (int)max_n_fwd[w], k, 1, w, S.st));
+                GB_CUDA_TRY(launch_ckpt_store(tab, cnt, (int)max_n_fwd[w], k, 1, w, S.st));
+                S.launches += q16 ? 2 : 1;
+            }
+            GB_CUDA_TRY(launch_step(w, kSrvTile, tab, cnt, max_tiles[w], k, S.st));
+            S.launches++;
+            if (k == S.sfe - 1 && cnt > nadj) {
+                if (q16) GB_CUDA_TRY(launch_ckpt_amax(tab, cnt, (int)max_n_fwd[w], k, 0, w, S.st));
+                GB_CUDA_TRY(launch_ckpt_store(tab, cnt, (int)max_n_fwd[w], k, 0, w, S.st));
+                S.launches += q16 ? 2 : 1;
+            }
+            if (k == 0 && nadj) {
+                GB_CUDA_TRY(launch_interaction(w, S.d_tab, S.d_grp + base, nadj, max_cells[w], k, S.st));
+                S.launches++;
+            }
+        }
+    }
+    for (Req *r : act) r->it += S.sfe;
+    S.rounds++;
+    return GB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+gb_server *gb_server_create(int sfe, int ckpt_precision, double hbm_budget_gb, int max_slots) {
+    if (sfe < 1 || ckpt_precision < 0 || ckpt_precision > 2) {
+        set_error("gb_server_create: sfe must be >= 1 and ckpt_precision 0, 1 or 2");
+        return nullptr;
+    }
+    gb_server *h = new gb_server();
+    Server &S = h->s;
+    S.sfe = sfe;
+    S.prec = ckpt_precision;
+    S.max_slots = max_slots > 0 ? max_slots : 1 << 20;
+    size_t freeb = 0, total = 0;
+    if (cudaStreamCreateWithFlags(&S.st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMemGetInfo(&freeb, &total) != cudaSuccess) {
+        set_error("gb_server_create: no CUDA device");
+        delete h;
+        return nullptr;
+    }
+    S.budget = hbm_budget_gb > 0 ? hbm_budget_gb * 1e9 : 0.8 * (double)freeb;
+    return h;
+}
+
+long long gb_server_submit(gb_server *h, const gb_request_desc *d) {
+    if (!h || !d || d->nx < 8 || d->nz < 8 || d->nt < 1 || !d->lambda || !d->mu || !d->rho || d->nrec < 0 ||
+        (d->nrec && !d->rec)) {
+        set_error("gb_server_submit: invalid request");
+        return -1;
+    }
+    Server &S = h->s;
+    if (d->nt % S.sfe) {
+        set_error("gb_server_submit: nt must be a multiple of the server's sfe");
+        return -1;
+    }
+    if (!(d->dx > 0) || !(d->dz > 0) || !(d->dt > 0)) {
+        set_error("gb_server_submit: dx, dz, dt must be positive");
+        return -1;
+    }
+    Req r;
+    r.id = (long long)S.reqs.size();
+    r.d = *d;
+    r.ncomp = d->psv ? 2 : 1;
+    r.nf = d->psv ? 4 : 2;
+    r.nsfe = d->nt / S.sfe;
+    r.bytes = S.footprint(*d, r.nf, r.nsfe, r.ncomp);
+    if ((double)r.bytes > S.budget) {
+        set_error("gb_server_submit: request needs " + std::to_string(r.bytes) + " bytes, more than the budget");
+        return -1;
+    }
+    S.reqs.push_back(r);
+    return r.id;
+}
+
+int gb_server_run(gb_server *h) {
+    if (!h) return GB_ERR_ARG;
+    Server &S = h->s;
+    std::vector<size_t> order(S.reqs.size());
+    for (size_t q = 0; q < order.size(); q++) order[q] = q;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](size_t a, size_t b) { return S.reqs[a].d.arrival < S.reqs[b].d.arrival; });
+    std::deque<size_t> waiting(order.begin(), order.end());
+    for (size_t q : order) {
+        S.reqs[q].phase = 0;
+        S.reqs[q].blk = nullptr;
+    }
+    std::vector<Req *> act;
+    const auto t0 = std::chrono::steady_clock::now();
+    size_t done = 0;
+    while (done < S.reqs.size()) {
+        // admission in arrival order, by HBM budget and free slots
+        while (!waiting.empty()) {
+            Req &r = S.reqs[waiting.front()];
+            if (r.d.arrival > now_s(t0)) break;
+            if ((int)act.size() >= S.max_slots || (double)(S.used + r.bytes) > S.budget) break;
+            int rc = admit(S, r);
+            if (rc) return rc;
+            r.t_admit = now_s(t0);
+            act.push_back(&r);
+            waiting.pop_front();
+        }
+        S.max_active = std::max(S.max_active, (int)act.size());
+        if (act.empty()) {
+            if (waiting.empty()) break;
+            const double wait = S.reqs[waiting.front()].d.arrival - now_s(t0);
+            if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(std::min(wait, 0.01)));
+            continue;
+        }
+        int rc = round_once(S, act);
+        if (rc) return rc;
+        // phase changes
+        std::vector<Req *> still;
+        for (Req *r : act) {
+            if (r->it < r->d.nt) {
+                still.push_back(r);
+                continue;
+            }
+            const gb_request_desc &d = r->d;
+            const size_t n = (size_t)d.nx * d.nz;
+            if (r->phase == 1) {
+                // waveform misfit and adjoint sources (misfit/waveform.h:4-40)
+                const int ntr = r->ncomp * d.nrec;
+                if (ntr) GB_CUDA_TRY(launch_waveform_refs(r->refs, r->tw, ntr, d.nt, std::sqrt(d.dt), r->val, S.st));
+                S.launches++;
+                std::vector<double> v(ntr);
+                if (ntr)
+                    GB_CUDA_TRY(cudaMemcpyAsync(v.data(), r->val, ntr * 8, cudaMemcpyDeviceToHost, S.st));
+                GB_CUDA_TRY(cudaMemsetAsync(r->state, 0, (size_t)(d.psv ? NPSV : NSH) * n * 4, S.st));
+                GB_CUDA_TRY(cudaStreamSynchronize(S.st));
+                r->misfit = 0;
+                for (double x : v) r->misfit += x;
+                r->phase = 2;
+                r->it = 0;
+                still.push_back(r);
+            } else {
+                for (int q = 0; q < 3; q++) {
+                    r->res[q].resize(n);
+                    GB_CUDA_TRY(cudaMemcpyAsync(r->res[q].data(), r->k[q], n * 4, cudaMemcpyDeviceToHost, S.st));
+                }
+                GB_CUDA_TRY(cudaFreeAsync(r->blk, S.st));
+                GB_CUDA_TRY(cudaFreeAsync(r->csr_src, S.st));
+                GB_CUDA_TRY(cudaStreamSynchronize(S.st));
+                r->blk = nullptr;
+                r->csr_src = nullptr;
+                r->t_done = now_s(t0);
+                r->phase = 3;
+                S.used -= r->bytes;
+                done++;
+            }
+        }
+        act.swap(still);
+    }
+    GB_CUDA_TRY(cudaStreamSynchronize(S.st));
+    S.run_s = now_s(t0);
+    return GB_OK;
+}
+
+int gb_server_result(gb_server *h, long long id, float *k_lambda, float *k_mu, float *k_rho, double *misfit,
+                     double *latency_s) {
+    if (!h || id < 0 || id >= (long long)h->s.reqs.size()) return GB_ERR_ARG;
+    Req &r = h->s.reqs[id];
+    if (r.phase != 3) {
+        set_error("gb_server_result: request not finished");
+        return GB_ERR_STATE;
+    }
+    float *outs[3] = {k_lambda, k_mu, k_rho};
+    for (int q = 0; q < 3; q++)
+        if (outs[q]) std::copy(r.res[q].begin(), r.res[q].end(), outs[q]);
+    if (misfit) *misfit = r.misfit;
+    if (latency_s) *latency_s = r.t_done - r.d.arrival;
+    return GB_OK;
+}
+
+int gb_server_report(gb_server *h, gb_server_stats *out) {
+    if (!h || !out) return GB_ERR_ARG;
+    Server &S = h->s;
+    std::vector<double> lat;
+    long long cells = 0;
+    for (auto &r : S.reqs)
+        if (r.phase == 3) {
+            lat.push_back(r.t_done - r.d.arrival);
+            cells += 2LL * r.d.nx * r.d.nz * r.d.nt;
+        }
+    std::sort(lat.begin(), lat.end());
+    auto pct = [&](double p) {
+        if (lat.empty()) return 0.0;
+        const size_t i = (size_t)std::min<double>(lat.size() - 1, std::ceil(p * lat.size()) - 1);
+        return lat[i];
+    };
+    memset(out, 0, sizeof *out);
+    out->completed = (int)lat.size();
+    out->wall_s = S.run_s;
+    out->p50_s = pct(0.50);
+    out->p99_s = pct(0.99);
+    out->max_concurrent = S.max_active;
+    out->rounds = S.rounds;
+    out->launches = S.launches;
+    out->cell_updates = cells;
+    return GB_OK;
+}
+
+void gb_server_destroy(gb_server *h) {
+    if (!h) return;
+    Server &S = h->s;
+    if (S.st) cudaStreamSynchronize(S.st);
+    for (auto &r : S.reqs) {
+        if (r.blk) cudaFree(r.blk);
+        if (r.csr_src) cudaFree(r.csr_src);
+    }
+    cudaFree(S.d_tab);
+    cudaFree(S.d_grp);
+    for (int b = 0; b < Server::kStage; b++) {
+        cudaFreeHost(S.h_tab[b]);
+        cudaFreeHost(S.h_grp[b]);
+        if (S.copied[b]) cudaEventDestroy(S.copied[b]);
+    }
+    if (S.st) cudaStreamDestroy(S.st);
+    delete h;
+}
+
+}  // extern "C"

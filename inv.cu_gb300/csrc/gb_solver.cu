@@ -507,6 +507,10 @@ int Solver::fill_slots(int kind, const int *shots, int n, bool record_u) {
         }
         if (psv)
             for (int f = 0; f < NPSV; f++) S.psv[f] = p + (size_t)f * nc;
+        S.it_base = 0;
+        S.par0 = 0;
+        S.sfe = sfe;
+        S.ckpt_write = kind == PASS_FWD;
         S.nsfe = nsfe;
         S.nf = nf();
         S.ckpt_prec = B.ckpt_prec < 0 ? CKPT_F32 : B.ckpt_prec;
@@ -569,7 +573,6 @@ int Solver::enqueue_pass(int kind, int n, bool snapshot, int snap_isrc) {
     win_steps = w1 - w0;
     const int nwave = (sh ? 1 : 0) + (psv ? 1 : 0);
     int par = 0;
-    const float ndt = (float)sfe * dt;
     for (int it = 0; it < nt; it++) {
         int isfe = -1;
         if (ck && (it + 1) % sfe == 0) isfe = nsfe - (it + 1) / sfe;
@@ -577,14 +580,14 @@ int Solver::enqueue_pass(int kind, int n, bool snapshot, int snap_isrc) {
             for (int w = 0; w < 2; w++) {
                 const bool wp = w == 1;
                 if (wp ? !psv : !sh) continue;
-                if (q16) GB_CUDA_TRY(launch_ckpt_amax(ds, n, (int)nc, isfe, 1, wp, par, st));
-                GB_CUDA_TRY(launch_ckpt_store(ds, n, (int)nc, isfe, 1, wp, par, st));
+                if (q16) GB_CUDA_TRY(launch_ckpt_amax(ds, n, (int)nc, it, 1, wp, st));
+                GB_CUDA_TRY(launch_ckpt_store(ds, n, (int)nc, it, 1, wp, st));
                 stats.launches += q16 ? 2 : 1;
             }
         }
         if (it == w0 && win_steps > 0) GB_CUDA_TRY(record_timing(ev_win0));
-        if (sh) GB_CUDA_TRY(launch_step(false, tile, ds, n, max_tiles(), it, par, st));
-        if (psv) GB_CUDA_TRY(launch_step(true, tile, ds, n, max_tiles(), it, par, st));
+        if (sh) GB_CUDA_TRY(launch_step(false, tile, ds, n, max_tiles(), it, st));
+        if (psv) GB_CUDA_TRY(launch_step(true, tile, ds, n, max_tiles(), it, st));
         stats.launches += nwave;
         if (it + 1 == w1 && win_steps > 0) GB_CUDA_TRY(record_timing(ev_win1));
         par ^= 1;
@@ -592,15 +595,14 @@ int Solver::enqueue_pass(int kind, int n, bool snapshot, int snap_isrc) {
             for (int w = 0; w < 2; w++) {
                 const bool wp = w == 1;
                 if (wp ? !psv : !sh) continue;
-                if (q16) GB_CUDA_TRY(launch_ckpt_amax(ds, n, (int)nc, isfe, 0, wp, par, st));
-                GB_CUDA_TRY(launch_ckpt_store(ds, n, (int)nc, isfe, 0, wp, par, st));
+                if (q16) GB_CUDA_TRY(launch_ckpt_amax(ds, n, (int)nc, it, 0, wp, st));
+                GB_CUDA_TRY(launch_ckpt_store(ds, n, (int)nc, it, 0, wp, st));
                 stats.launches += q16 ? 2 : 1;
             }
         }
         if (kind == PASS_ADJ && sfe > 0 && it % sfe == 0) {
-            const int isfe_a = it / sfe;
-            if (sh) GB_CUDA_TRY(launch_interaction(false, ds, d_group, 1, (int)nc, isfe_a, ndt, par, st));
-            if (psv) GB_CUDA_TRY(launch_interaction(true, ds, d_group, 1, (int)nc, isfe_a, ndt, par, st));
+            if (sh) GB_CUDA_TRY(launch_interaction(false, ds, d_group, 1, (int)nc, it, st));
+            if (psv) GB_CUDA_TRY(launch_interaction(true, ds, d_group, 1, (int)nc, it, st));
             stats.launches += nwave;
         }
         if (snapshot) {
@@ -637,8 +639,8 @@ int Solver::autotune(int n) {
         const int reps = 8;
         for (int r = 0; r < 3 + reps; r++) {
             if (r == 3) GB_CUDA_TRY(cudaEventRecord(ev_win0, st));
-            if (sh) GB_CUDA_TRY(launch_step(false, tc, d_tune, n, mt, r, r & 1, st));
-            if (psv) GB_CUDA_TRY(launch_step(true, tc, d_tune, n, mt, r, r & 1, st));
+            if (sh) GB_CUDA_TRY(launch_step(false, tc, d_tune, n, mt, r, st));
+            if (psv) GB_CUDA_TRY(launch_step(true, tc, d_tune, n, mt, r, st));
         }
         GB_CUDA_TRY(cudaEventRecord(ev_win1, st));
         GB_CUDA_TRY(cudaEventSynchronize(ev_win1));

@@ -65,7 +65,7 @@ __device__ __forceinline__ void cp_async_wait_all() {
 constexpr int kMaxInjTraces = 128;  // source samples staged in shared memory per tile
 
 template <bool PSV, int TZ, int TX>
-__global__ void __launch_bounds__(kThreads) k_step(const Slot *__restrict__ slots, int it, int par) {
+__global__ void __launch_bounds__(kThreads) k_step(const Slot *__restrict__ slots, int kstep) {
     constexpr int NS = PSV ? 3 : 2;  // stress components held in shared memory
     constexpr int NV = PSV ? 2 : 1;  // velocity components
     constexpr int RZ = TZ + 6, RX = TX + 6;
@@ -81,6 +81,9 @@ __global__ void __launch_bounds__(kThreads) k_step(const Slot *__restrict__ slot
 
     const Slot &S = slots[blockIdx.y];
     if (!S.active) return;
+    const int it = S.it_base + kstep;
+    if (it < 0 || it >= S.nt) return;
+    const int par = (S.par0 + kstep) & 1;
     const int nx = S.nx, nz = S.nz;
     const int tile = blockIdx.x;
     if (tile >= S.tiles_z * S.tiles_x) return;
@@ -335,30 +338,30 @@ __global__ void __launch_bounds__(kThreads) k_step(const Slot *__restrict__ slot
 }
 
 template <bool PSV>
-static cudaError_t launch_step_t(TileCfg tc, const Slot *d_slots, int nslots, int max_tiles, int it, int par,
+static cudaError_t launch_step_t(TileCfg tc, const Slot *d_slots, int nslots, int max_tiles, int k,
                                  cudaStream_t st) {
     dim3 grid(max_tiles, nslots);
     if (tc.tz == 32 && tc.tx == 32)
-        k_step<PSV, 32, 32><<<grid, kThreads, 0, st>>>(d_slots, it, par);
+        k_step<PSV, 32, 32><<<grid, kThreads, 0, st>>>(d_slots, k);
     else if (tc.tz == 64 && tc.tx == 16)
-        k_step<PSV, 64, 16><<<grid, kThreads, 0, st>>>(d_slots, it, par);
+        k_step<PSV, 64, 16><<<grid, kThreads, 0, st>>>(d_slots, k);
     else if (tc.tz == 32 && tc.tx == 16)
-        k_step<PSV, 32, 16><<<grid, kThreads, 0, st>>>(d_slots, it, par);
+        k_step<PSV, 32, 16><<<grid, kThreads, 0, st>>>(d_slots, k);
     else if (tc.tz == 16 && tc.tx == 32)
-        k_step<PSV, 16, 32><<<grid, kThreads, 0, st>>>(d_slots, it, par);
+        k_step<PSV, 16, 32><<<grid, kThreads, 0, st>>>(d_slots, k);
     else if (tc.tz == 128 && tc.tx == 8)
-        k_step<PSV, 128, 8><<<grid, kThreads, 0, st>>>(d_slots, it, par);
+        k_step<PSV, 128, 8><<<grid, kThreads, 0, st>>>(d_slots, k);
     else
         return cudaErrorInvalidValue;
     return cudaGetLastError();
 }
 
-cudaError_t launch_step(bool psv, TileCfg tc, const Slot *d_slots, int nslots, int max_tiles, int it, int par,
+cudaError_t launch_step(bool psv, TileCfg tc, const Slot *d_slots, int nslots, int max_tiles, int k,
                         cudaStream_t st) {
     if (nslots <= 0 || max_tiles <= 0) return cudaSuccess;
-    if (tc.threads) return launch_march(psv, tc.threads, tc.tx, d_slots, nslots, max_tiles, it, par, st);
-    return psv ? launch_step_t<true>(tc, d_slots, nslots, max_tiles, it, par, st)
-               : launch_step_t<false>(tc, d_slots, nslots, max_tiles, it, par, st);
+    if (tc.threads) return launch_march(psv, tc.threads, tc.tx, d_slots, nslots, max_tiles, k, st);
+    return psv ? launch_step_t<true>(tc, d_slots, nslots, max_tiles, k, st)
+               : launch_step_t<false>(tc, d_slots, nslots, max_tiles, k, st);
 }
 
 // ------------------------------------------------------------ checkpoints
@@ -401,9 +404,23 @@ __device__ __forceinline__ int ckpt_fields(const Slot &S, bool psv, int which_u,
     return 2;
 }
 
-__global__ void k_ckpt_amax(const Slot *__restrict__ slots, int isfe, int which_u, bool psv, int par) {
+// Checkpoint slot of step index k for slot S, or -1 when k is not a
+// checkpoint step of S; *par receives the parity of the velocity written by
+// that step.
+__device__ __forceinline__ int ckpt_slot(const Slot &S, int k, int *par) {
+    if (!S.active || !S.ckpt || !S.ckpt_write || S.sfe <= 0) return -1;
+    const int it = S.it_base + k;
+    if (it < 0 || it >= S.nt || (it + 1) % S.sfe != 0) return -1;
+    const int isfe = S.nsfe - (it + 1) / S.sfe;
+    *par = (S.par0 + k + 1) & 1;
+    return (isfe >= 0 && isfe < S.nsfe) ? isfe : -1;
+}
+
+__global__ void k_ckpt_amax(const Slot *__restrict__ slots, int kstep, int which_u, bool psv) {
     const Slot &S = slots[blockIdx.y];
-    if (!S.active || !S.ckpt || isfe < 0 || isfe >= S.nsfe) return;
+    int par = 0;
+    const int isfe = ckpt_slot(S, kstep, &par);
+    if (isfe < 0) return;
     if (psv ? S.psv[0] == nullptr : S.sh[0] == nullptr) return;
     const float *src[2];
     int q[2];
@@ -429,9 +446,11 @@ __global__ void k_ckpt_amax(const Slot *__restrict__ slots, int isfe, int which_
     }
 }
 
-__global__ void k_ckpt_store(const Slot *__restrict__ slots, int isfe, int which_u, bool psv, int par) {
+__global__ void k_ckpt_store(const Slot *__restrict__ slots, int kstep, int which_u, bool psv) {
     const Slot &S = slots[blockIdx.y];
-    if (!S.active || !S.ckpt || isfe < 0 || isfe >= S.nsfe) return;
+    int par = 0;
+    const int isfe = ckpt_slot(S, kstep, &par);
+    if (isfe < 0) return;
     if (psv ? S.psv[0] == nullptr : S.sh[0] == nullptr) return;
     const float *src[2];
     int q[2];
@@ -463,17 +482,17 @@ static int ckpt_blocks(int n) {
     return b < 1 ? 1 : (b > 1216 ? 1216 : b);
 }
 
-cudaError_t launch_ckpt_amax(const Slot *d_slots, int nslots, int n, int isfe, int which_u, bool psv, int par,
+cudaError_t launch_ckpt_amax(const Slot *d_slots, int nslots, int n, int k, int which_u, bool psv,
                              cudaStream_t st) {
     if (nslots <= 0) return cudaSuccess;
-    k_ckpt_amax<<<dim3(ckpt_blocks(n), nslots), 256, 0, st>>>(d_slots, isfe, which_u, psv, par);
+    k_ckpt_amax<<<dim3(ckpt_blocks(n), nslots), 256, 0, st>>>(d_slots, k, which_u, psv);
     return cudaGetLastError();
 }
 
-cudaError_t launch_ckpt_store(const Slot *d_slots, int nslots, int n, int isfe, int which_u, bool psv, int par,
+cudaError_t launch_ckpt_store(const Slot *d_slots, int nslots, int n, int k, int which_u, bool psv,
                               cudaStream_t st) {
     if (nslots <= 0) return cudaSuccess;
-    k_ckpt_store<<<dim3(ckpt_blocks(n), nslots), 256, 0, st>>>(d_slots, isfe, which_u, psv, par);
+    k_ckpt_store<<<dim3(ckpt_blocks(n), nslots), 256, 0, st>>>(d_slots, k, which_u, psv);
     return cudaGetLastError();
 }
 
@@ -492,8 +511,7 @@ __device__ __forceinline__ float ck_load(const Slot &S, int isfe, int q, size_t 
 }
 
 template <bool PSV>
-__global__ void k_interaction(const Slot *__restrict__ slots, const KernelGroup *__restrict__ groups, int isfe,
-                              float ndt, int par) {
+__global__ void k_interaction(const Slot *__restrict__ slots, const KernelGroup *__restrict__ groups, int kstep) {
     const KernelGroup &G = groups[blockIdx.y];
     const int nx = G.nx, nz = G.nz;
     const size_t n = (size_t)nx * nz;
@@ -506,7 +524,13 @@ __global__ void k_interaction(const Slot *__restrict__ slots, const KernelGroup 
     float kr = G.inv_rho ? G.k_rho[k] : 0.f;
     for (int s = G.first; s < G.first + G.count; s++) {
         const Slot &S = slots[s];
-        if (!S.active || !S.ckpt) continue;
+        if (!S.active || !S.ckpt || S.sfe <= 0) continue;
+        const int it = S.it_base + kstep;
+        if (it < 0 || it >= S.nt || it % S.sfe != 0) continue;
+        const int isfe = it / S.sfe;
+        if (isfe >= S.nsfe) continue;
+        const int par = (S.par0 + kstep + 1) & 1;  // velocity written by this step
+        const float ndt = (float)S.sfe * S.dt;
         const float c9x = S.c9x, c24x = S.c24x, c9z = S.c9z, c24z = S.c24z;
         const int base = (PSV && S.sh[0] != nullptr) ? 2 : 0;
         const int nfu = PSV ? 2 : 1;
@@ -561,13 +585,13 @@ __global__ void k_interaction(const Slot *__restrict__ slots, const KernelGroup 
 }
 
 cudaError_t launch_interaction(bool psv, const Slot *d_slots, const KernelGroup *d_groups, int ngroups,
-                               int max_cells, int isfe, float ndt, int par, cudaStream_t st) {
+                               int max_cells, int k, cudaStream_t st) {
     if (ngroups <= 0) return cudaSuccess;
     dim3 grid((max_cells + 255) / 256, ngroups);
     if (psv)
-        k_interaction<true><<<grid, 256, 0, st>>>(d_slots, d_groups, isfe, ndt, par);
+        k_interaction<true><<<grid, 256, 0, st>>>(d_slots, d_groups, k);
     else
-        k_interaction<false><<<grid, 256, 0, st>>>(d_slots, d_groups, isfe, ndt, par);
+        k_interaction<false><<<grid, 256, 0, st>>>(d_slots, d_groups, k);
     return cudaGetLastError();
 }
 

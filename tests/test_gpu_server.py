@@ -1,0 +1,88 @@
+"""Serving engine: continuous batching of forward+adjoint requests with
+different grids, step counts and wave systems. Each result must be the same
+alone and in the mix (bit-identical: the same operations in the same order),
+match the CPU oracle, and admission must respect the HBM budget."""
+import numpy as np
+import pytest
+
+from tests import cases
+
+pytestmark = pytest.mark.gpu
+
+
+def request(psv, nx, nz, nt, seed, nrec=24):
+    case = cases.make_case(wave="psv" if psv else "sh", nx=nx, nz=nz, nt=nt, nsrc=1, nrec=nrec, sfe=10,
+                           seed=seed, abs_width=10)
+    vp, vs, rho = case["vp"], case["vs"], case["rho"]
+    f32 = np.float32
+    lam = np.where(vp > vs, (rho * (vp * vp - f32(2) * vs * vs)).astype(f32), f32(0)).astype(f32)
+    mu = (rho * vs * vs).astype(f32)
+    req = dict(psv=int(psv), nx=nx, nz=nz, dx=10.0, dt=case["dt"], nt=nt, lam=lam, mu=mu, rho=rho,
+               src=case["src"][0], rec=np.array(case["rec"], np.float32), abs_width=10)
+    return case, req
+
+
+MIX = [(1, 90, 70, 300, 1), (0, 120, 64, 200, 2), (1, 64, 96, 400, 3), (0, 80, 80, 300, 4),
+       (1, 110, 50, 200, 5), (0, 70, 100, 400, 6)]
+
+
+def test_results_same_alone_and_in_the_mix(gpu):
+    reqs = [request(*m)[1] for m in MIX]
+    srv = gpu.Server(sfe=10)
+    ids = [srv.submit(arrival=0.002 * q, **r) for q, r in enumerate(reqs)]
+    srv.run()
+    st = srv.stats()
+    assert st.completed == len(MIX)
+    assert st.max_concurrent >= 3  # requests overlapped on the device
+    mix = [srv.result(i) for i in ids]
+    for q, r in enumerate(reqs):
+        alone = gpu.Server(sfe=10)
+        rid = alone.submit(**r)
+        alone.run()
+        res = alone.result(rid)
+        for name in ("k_lambda", "k_mu", "k_rho"):
+            np.testing.assert_array_equal(res[name], mix[q][name])
+        assert res["misfit"] == mix[q]["misfit"]
+        assert np.abs(mix[q]["k_mu"]).max() > 0
+
+
+@pytest.mark.parametrize("psv", [1, 0])
+def test_served_request_matches_oracle(gpu, orc, psv):
+    case, req = request(psv, 96, 72, 300, 11)
+    pb = cases.oracle_problem(orc, case)
+    rng = np.random.default_rng(5)
+    comps = "xz" if psv else "y"
+    obs = {c: (rng.standard_normal((pb.nrec, pb.nt)) * 1e-9).astype(np.float32) for c in comps}
+    srv = gpu.Server(sfe=10)
+    rid = srv.submit(obs=np.stack([obs[c] for c in comps]), **req)
+    srv.run()
+    res = srv.result(rid)
+    o = orc.forward(pb, 0, adj=True)
+    tw = orc.taper(pb.nt, case["dt"])
+    ad = {c: np.zeros((pb.nrec, pb.nt), np.float32) for c in "xyz"}
+    total = 0.0
+    for c in comps:
+        v, ad[c] = orc.waveform_misfit(o["xyz".index(c)], obs[c], tw, case["dt"])
+        total += v
+    kern = orc.adjoint(pb, [ad["x"], ad["y"], ad["z"]], o[3])
+    assert abs(res["misfit"] - total) / total < 1e-4
+    names = ("k_lambda", "k_mu", "k_rho") if psv else ("k_mu", "k_rho")
+    for name in names:
+        ref = kern[("k_lambda", "k_mu", "k_rho").index(name)]
+        assert cases.rel(res[name], ref) < 1e-4, name
+
+
+def test_admission_waits_for_memory(gpu):
+    reqs = [request(1, 100, 80, 300, 20 + q)[1] for q in range(4)]
+    # each request needs about 5 MB (mostly checkpoints); 7 MB admits one at a time
+    srv = gpu.Server(sfe=10, hbm_budget_gb=0.007)
+    ids = [srv.submit(**r) for r in reqs]
+    srv.run()
+    st = srv.stats()
+    assert st.completed == 4 and st.max_concurrent == 1
+    free = gpu.Server(sfe=10)
+    fid = [free.submit(**r) for r in reqs]
+    free.run()
+    assert free.stats().max_concurrent == 4
+    for a, b in zip(ids, fid):
+        np.testing.assert_array_equal(srv.result(a)["k_mu"], free.result(b)["k_mu"])
