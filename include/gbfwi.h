@@ -134,8 +134,11 @@ int gb_run_adjoint_batch(gb_solver *s, const int *isrc, int n);
 float *gb_slot_ptr(gb_solver *s, int slot, int which);
 int gb_solver_batch_capacity(gb_solver *s);
 /* Runtime options: "batch" (slots, 0 = from the HBM budget), "graphs" (0/1),
- * "ckpt" (0 FP32, 1 BF16, 2 FP16), "tile" (0 autotune, 1..5 fixed),
- * "hbm_budget_gb". Options change no numerical result except "ckpt". */
+ * "ckpt" (0 FP32, 1 BF16, 2 FP16), "tile" (0 autotune, 1..20 fixed),
+ * "cluster" (1: run whole passes in thread-block clusters when a shot's
+ * state fits in their shared memory, 0: never), "hbm_budget_gb". Options
+ * change no forward result; "ckpt" changes kernels by the checkpoint
+ * rounding and "cluster" by the order in which shots are summed. */
 int gb_solver_set_option(gb_solver *s, const char *key, double value);
 
 /* Timing of the solver since the last reset (CUDA events on the solver's

@@ -302,6 +302,8 @@ int gb_solver_set_option(gb_solver *s, const char *key, double value) {
         v.opt_tile = t;
         if (t == 0) v.tile_id = 0;
         v.invalidate_graphs();
+    } else if (k == "cluster") {
+        v.opt_cluster = value != 0;
     } else if (k == "hbm_budget_gb") {
         if (v.capacity) {
             set_error("option hbm_budget_gb: set it before the first run");

@@ -6,6 +6,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <math.h>
 #include <stdint.h>
 
 #include <string>
@@ -35,6 +36,11 @@ struct Slot {
     int it_base, par0;
     int sfe;         // checkpoint spacing (steps)
     int ckpt_write;  // 1: forward pass stores checkpoints; 0: adjoint reads them
+    // cluster-resident path: forward source cell and trace (src_trace < 0:
+    // none), receiver cells (distinct)
+    int src_i, src_j, src_trace;
+    const int *pts_i, *pts_j;
+    int npts;
     float dt;
     float c9x, c24x, c9z, c24z;  // 9/(8h) and 1/(24h) for h = dx, dz
     const float *lambda, *mu, *rho;
@@ -70,6 +76,26 @@ struct TileCfg {
     int tz, tx, threads;
 };
 
+// Cluster-resident solver geometry: R CTAs per shot (cluster), cols_per grid
+// columns per CTA, rows_pad = nz rounded up to 32, G column groups per CTA
+// (blockDim = rows_pad * G).
+struct ClusterGeom {
+    int R, cols_per, G, rows_pad;
+};
+
+// Power-of-two scale of a 16-bit checkpoint with max |value| amax: FP16 maps
+// amax to at most 2^15, BF16 to at most 1; FP32 and empty fields use 1.
+#ifdef __CUDACC__
+__host__ __device__
+#endif
+inline float ckpt_scale_of(float amax, int prec) {
+    if (!(amax > 0.f) || prec == 0) return 1.f;
+    const float target = prec == 2 ? 32768.f : 1.f;
+    int e;
+    frexpf(target / amax, &e);
+    return ldexpf(1.f, e - 1);
+}
+
 // Packed tile CSR header: [0]=ntiles [1]=nentries [2]=ntraces, then
 // tile_ptr[ntiles+1], local[nentries], tptr[nentries+1], traces[ntraces].
 inline int csr_words(int ntiles, int nent, int ntr) { return 3 + ntiles + 1 + nent + nent + 1 + ntr; }
@@ -92,6 +118,14 @@ cudaError_t launch_ckpt_store(const Slot *d_slots, int nslots, int n, int k, int
 cudaError_t launch_interaction(bool psv, const Slot *d_slots, const KernelGroup *d_groups, int ngroups,
                                int max_cells, int k, cudaStream_t st);
 cudaError_t launch_fill(float *p, float v, size_t n, cudaStream_t st);
+// Cluster-resident passes (gb_cluster.cu): one cluster per slot runs the
+// whole pass; the adjoint adds each slot's kernels to kpart[slot][3][nx*nz].
+size_t cluster_smem_bytes(bool psv, const ClusterGeom &g, int nz);
+int cluster_occupancy(bool psv, ClusterGeom g, int nz);
+cudaError_t launch_cluster(bool psv, bool adj, const Slot *d_slots, int nslots, ClusterGeom g, int nz, float *kpart,
+                           cudaStream_t st);
+cudaError_t launch_cluster_reduce(const float *kpart, int nslots, size_t ncell, float *kl, float *km, float *kr,
+                                  int inv_l, int inv_m, int inv_r, cudaStream_t st);
 cudaError_t launch_mesh2grid(float *lambda, float *mu, float *rho, const float *px, const float *pz,
                              const float *pa, const float *pb, const float *pr, int npt, float dmax, float dx,
                              float dz, int nx, int nz, cudaStream_t st);

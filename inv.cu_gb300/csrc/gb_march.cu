@@ -22,14 +22,15 @@
 // Arithmetic, guards and update order are those of the 2-D tile kernel
 // (solver/fdm.h:76-161): results do not depend on T, C or batching.
 #include "gb_internal.h"
+#include "gb_stencil.h"
 
 namespace gb {
 
 __device__ __forceinline__ float dminus_m(float a0, float am1, float ap1, float am2, float c9, float c24) {
-    return fmaf(a0 - am1, c9, -((ap1 - am2) * c24));
+    return st_dminus(a0, am1, ap1, am2, c9, c24);
 }
 __device__ __forceinline__ float dplus_m(float ap1, float a0, float ap2, float am1, float c9, float c24) {
-    return fmaf(ap1 - a0, c9, -((ap2 - am1) * c24));
+    return st_dplus(ap1, a0, ap2, am1, c9, c24);
 }
 
 struct CsrM {
@@ -283,13 +284,13 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
                 const float ab = cur[W::AX] * azj;
                 const float rinv = cur[W::RHO];
 #pragma unroll
-                for (int f = 0; f < NV; f++) vn[f] = ab * fmaf(dt * ds[f], rinv, cur[W::V + f]);
+                for (int f = 0; f < NV; f++) vn[f] = st_velocity(ab, dt, ds[f], rinv, cur[W::V + f]);
             }
             if (pv >= c0 && pv < c1) {
                 const int oc = pv - c0;
                 float un[NV];
 #pragma unroll
-                for (int f = 0; f < NV; f++) un[f] = cur[W::U + f] + vn[f] * dt;
+                for (int f = 0; f < NV; f++) un[f] = st_displacement(cur[W::U + f], vn[f], dt);
                 if (rowown) {
                     const int kv = pv * nz + j;
 #pragma unroll
@@ -344,16 +345,18 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
                 const float dvxdx = xV ? dplus_m(vq[2][0], vq[1][0], vq[3][0], vq[0][0], c9x, c24x) : 0.f;
                 const float dvzdx = xV ? dplus_m(vq[2][1], vq[1][1], vq[3][1], vq[0][1], c9x, c24x) : 0.f;
                 const float dvxdz = dzq[0][0], dvzdz = dzq[0][1];
-                const float l = cur[W::LAM];
-                const float l2m = l + 2.f * m;
-                sig_out[0][km] = sq[0][0] + dt * (l2m * dvxdx + l * dvzdz);
-                sig_out[1][km] = sq[0][1] + dt * (l2m * dvzdz + l * dvxdx);
-                sig_out[2][km] = sq[0][2] + dt * (m * (dvxdz + dvzdx));
+                float sxx = sq[0][0], szz = sq[0][1], sxz = sq[0][2];
+                st_stress_psv(sxx, szz, sxz, cur[W::LAM], m, dt, dvxdx, dvxdz, dvzdx, dvzdz);
+                sig_out[0][km] = sxx;
+                sig_out[1][km] = szz;
+                sig_out[2][km] = sxz;
             } else {
                 const float dvydx = xV ? dplus_m(vq[2][0], vq[1][0], vq[3][0], vq[0][0], c9x, c24x) : 0.f;
                 const float dvydz = dzq[0][0];
-                sig_out[0][km] = sq[0][0] + dt * m * dvydx;
-                sig_out[1][km] = sq[0][1] + dt * m * dvydz;
+                float sxy = sq[0][0], szy = sq[0][1];
+                st_stress_sh(sxy, szy, m, dt, dvydx, dvydz);
+                sig_out[0][km] = sxy;
+                sig_out[1][km] = szy;
             }
         }
     }

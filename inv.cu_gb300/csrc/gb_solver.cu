@@ -168,6 +168,7 @@ int Solver::init(const Config &cfg, int nx_, int nz_, float xmax_, float zmax_) 
     if (cfg.has("graphs")) opt_graphs = cfg.iv("graphs") != 0;
     if (cfg.has("ckpt_precision")) opt_ckpt = cfg.iv("ckpt_precision");
     if (cfg.has("tile")) opt_tile = cfg.iv("tile");
+    if (cfg.has("cluster")) opt_cluster = cfg.iv("cluster") != 0;
     nx = nx_;
     nz = nz_;
     xmax = xmax_;
@@ -245,6 +246,19 @@ int Solver::init(const Config &cfg, int nx_, int nz_, float xmax_, float zmax_) 
     GB_CUDA_TRY(cudaMalloc(&az, nz * 4));
     GB_CUDA_TRY(cudaMemcpy(ax, hax.data(), nx * 4, cudaMemcpyHostToDevice));
     GB_CUDA_TRY(cudaMemcpy(az, haz.data(), nz * 4, cudaMemcpyHostToDevice));
+    {
+        std::vector<int> cells(2 * (size_t)std::max(nrec, 1), 0);
+        std::vector<long long> keys;
+        for (int r = 0; r < nrec; r++) {
+            cells[r] = rec_xi[r];
+            cells[nrec + r] = rec_zi[r];
+            keys.push_back((long long)rec_xi[r] * (nz + 1) + rec_zi[r]);
+        }
+        std::sort(keys.begin(), keys.end());
+        rec_distinct = std::adjacent_find(keys.begin(), keys.end()) == keys.end();
+        GB_CUDA_TRY(cudaMalloc(&d_rec_cells, cells.size() * 4));
+        GB_CUDA_TRY(cudaMemcpy(d_rec_cells, cells.data(), cells.size() * 4, cudaMemcpyHostToDevice));
+    }
     GB_CUDA_TRY(cudaMalloc(&d_group, sizeof(KernelGroup)));
     GB_CUDA_TRY(cudaMallocHost(&h_group, sizeof(KernelGroup)));
     stats = gb_stats{};
@@ -273,6 +287,8 @@ void Solver::release() {
     cudaFree(d_group);
     cudaFreeHost(h_group);
     cudaFree(d_csr);
+    cudaFree(d_rec_cells);
+    cudaFree(kpart);
     for (cudaEvent_t e : {ev_pass0, ev_pass1, ev_win0, ev_win1, ev_t0, ev_t1})
         if (e) cudaEventDestroy(e);
     if (st) cudaStreamDestroy(st);
@@ -509,6 +525,10 @@ int Solver::fill_slots(int kind, const int *shots, int n, bool record_u) {
             for (int f = 0; f < NPSV; f++) S.psv[f] = p + (size_t)f * nc;
         S.it_base = 0;
         S.par0 = 0;
+        S.pts_i = d_rec_cells;
+        S.pts_j = d_rec_cells + nrec;
+        S.npts = nrec;
+        S.src_trace = -1;
         S.sfe = sfe;
         S.ckpt_write = kind == PASS_FWD;
         S.nsfe = nsfe;
@@ -524,6 +544,11 @@ int Solver::fill_slots(int kind, const int *shots, int n, bool record_u) {
         } else {
             const int is = shots[b];
             S.inj = nsrc ? d_csr + (is >= 0 ? src_set[is] : super_set) : nullptr;
+            if (is >= 0 && nsrc) {
+                S.src_i = src_xi[is];
+                S.src_j = src_zi[is];
+                S.src_trace = is;
+            }
             S.inj_x = stf[0];
             S.inj_y = stf[1];
             S.inj_z = stf[2];
@@ -712,6 +737,93 @@ int Solver::run_pass(int kind, int n, bool snapshot, int snap_isrc) {
     return GB_OK;
 }
 
+// Cluster geometry for one wave system: R CTAs per shot, each holding
+// cols_per columns of the state (plus a receiver map) in shared memory.
+// Chooses the R with the fewest (cluster rounds x columns per thread).
+bool Solver::cluster_geometry(bool wave_psv, int n, ClusterGeom *out) const {
+    if (nz > 1024 || nx < 2) return false;
+    const int rows_pad = (nz + 31) / 32 * 32;
+    const int gmax = 1024 / rows_pad;
+    const size_t limit = 227 * 1024;
+    long best = -1;
+    for (int R = 2; R <= 16; R++) {
+        ClusterGeom g;
+        g.R = R;
+        g.cols_per = (nx + R - 1) / R;
+        g.rows_pad = rows_pad;
+        g.G = std::min(gmax, g.cols_per);
+        if (g.cols_per < 3 || cluster_smem_bytes(wave_psv, g, nz) > limit) continue;
+        const int occ = cluster_occupancy(wave_psv, g, nz);
+        if (occ < 1) continue;
+        const long cost = (long)((n + occ - 1) / occ) * ((g.cols_per + g.G - 1) / g.G);
+        if (best < 0 || cost < best) {
+            best = cost;
+            *out = g;
+        }
+    }
+    return best >= 0;
+}
+
+bool Solver::cluster_ok(const int *shots, int n, bool snapshot) const {
+    if (!opt_cluster || snapshot || !rec_distinct || opt_ckpt != CKPT_F32) return false;
+    for (int b = 0; b < n; b++)
+        if (shots[b] < 0) return false;
+    ClusterGeom g;
+    if (sh && !cluster_geometry(false, n, &g)) return false;
+    if (psv && !cluster_geometry(true, n, &g)) return false;
+    return true;
+}
+
+// One pass with the cluster-resident kernel: one launch per wave system.
+int Solver::run_cluster_pass(int kind, int n) {
+    const size_t nc = ncell();
+    GB_CUDA_TRY(cudaEventRecord(ev_pass0, st));
+    GB_CUDA_TRY(launch_reciprocal(rinv, rho, nc, st));
+    const bool adjp = kind == PASS_ADJ;
+    if (adjp) {
+        if (kpart_slots < (size_t)n) {
+            GB_CUDA_TRY(cudaStreamSynchronize(st));
+            cudaFree(kpart);
+            GB_CUDA_TRY(cudaMalloc(&kpart, (size_t)n * 3 * nc * 4));
+            kpart_slots = n;
+        }
+        GB_CUDA_TRY(cudaMemsetAsync(kpart, 0, (size_t)n * 3 * nc * 4, st));
+    }
+    for (int w = 0; w < 2; w++) {
+        const bool wp = w == 1;
+        if (wp ? !psv : !sh) continue;
+        ClusterGeom g;
+        if (!cluster_geometry(wp, n, &g)) {
+            set_error("cluster pass: no geometry fits");
+            return GB_ERR_STATE;
+        }
+        GB_CUDA_TRY(launch_cluster(wp, adjp, d_slots[kind], n, g, nz, adjp ? kpart : nullptr, st));
+        stats.launches += 1;
+        if (adjp) {
+            GB_CUDA_TRY(launch_cluster_reduce(kpart, n, nc, k_lambda, k_mu, k_rho, wp && inv_lambda, inv_mu, inv_rho,
+                                              st));
+            GB_CUDA_TRY(cudaMemsetAsync(kpart, 0, (size_t)n * 3 * nc * 4, st));
+            stats.launches += 1;
+        }
+        stats.tile_tz = -g.R;
+        stats.tile_tx = g.cols_per;
+    }
+    GB_CUDA_TRY(cudaEventRecord(ev_pass1, st));
+    GB_CUDA_TRY(cudaStreamSynchronize(st));
+    float ms = 0;
+    GB_CUDA_TRY(cudaEventElapsedTime(&ms, ev_pass0, ev_pass1));
+    if (adjp)
+        stats.adjoint_ms += ms;
+    else
+        stats.forward_ms += ms;
+    // the whole pass is one kernel per system: book it as nt steps
+    stats.step_ms += ms;
+    stats.step_launches += nt;
+    stats.cell_updates += (long long)nc * nt * n;
+    last_par = nt & 1;
+    return GB_OK;
+}
+
 int Solver::forward(const int *shots, int n, bool ckpt_on, bool record_u, bool snapshot) {
     if (n < 1) return GB_OK;
     for (int b = 0; b < n; b++)
@@ -744,6 +856,7 @@ int Solver::forward(const int *shots, int n, bool ckpt_on, bool record_u, bool s
     rc = fill_slots(kind, shots, n, record_u);
     if (rc) return rc;
     last_forward_n = n;
+    if (cluster_ok(shots, n, snapshot)) return run_cluster_pass(kind, n);
     return run_pass(kind, n, snapshot, -1);
 }
 
@@ -776,6 +889,7 @@ int Solver::adjoint(const int *shots, int n, bool snapshot, int snap_isrc) {
     G.nx = nx;
     G.nz = nz;
     GB_CUDA_TRY(cudaMemcpyAsync(d_group, h_group, sizeof(KernelGroup), cudaMemcpyHostToDevice, st));
+    if (cluster_ok(shots, n, snapshot)) return run_cluster_pass(PASS_ADJ, n);
     return run_pass(PASS_ADJ, n, snapshot, snap_isrc);
 }
 

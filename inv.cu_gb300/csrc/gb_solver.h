@@ -59,6 +59,7 @@ struct Solver {
     int opt_ckpt = CKPT_F32;
     int opt_tile = 0;  // 0 = autotune
     double opt_budget_gb = 0;
+    bool opt_cluster = true;  // cluster-resident passes when the state fits on chip
 
     // device buffers in the reference layout
     float *lambda = nullptr, *mu = nullptr, *rho = nullptr;
@@ -66,6 +67,10 @@ struct Solver {
     float *k_lambda = nullptr, *k_mu = nullptr, *k_rho = nullptr;
     float *stf[3] = {nullptr, nullptr, nullptr};
     float *ax = nullptr, *az = nullptr;
+    int *d_rec_cells = nullptr;   // receiver cells: i[nrec] then j[nrec]
+    bool rec_distinct = true;     // no two receivers share a cell
+    float *kpart = nullptr;       // per-slot kernel contributions (cluster adjoint)
+    size_t kpart_slots = 0;
 
     // batch slots
     std::vector<SlotBuf> slots;
@@ -114,6 +119,9 @@ struct Solver {
     int enqueue_pass(int kind, int n, bool snapshot, int snap_isrc);
     int run_pass(int kind, int n, bool snapshot, int snap_isrc);
     int autotune(int n);
+    bool cluster_geometry(bool wave_psv, int n, ClusterGeom *g) const;
+    bool cluster_ok(const int *shots, int n, bool snapshot) const;
+    int run_cluster_pass(int kind, int n);
     int export_snapshot(int it, int isrc, int par);
     int export_data(const std::string &comp, const float *d_data, int n);
     void invalidate_graphs();

@@ -1,0 +1,41 @@
+// Per-cell arithmetic of the time step, shared by every step kernel (2-D
+// tile, marching strip, cluster-resident) so that they compute bit-identical
+// results. Every multiply-add is an explicit fmaf: the result does not depend
+// on how the compiler would contract a plain expression in each kernel.
+//
+// The operations follow the reference (solver/fdm.h:76-161); its divisions by
+// 8h, 24h and rho are multiplications by 9/(8h), 1/(24h) and 1/rho here.
+#pragma once
+
+namespace gb {
+
+// Backward-staggered difference at k: 9(a0 - am1)/(8h) - (ap1 - am2)/(24h).
+__device__ __forceinline__ float st_dminus(float a0, float am1, float ap1, float am2, float c9, float c24) {
+    return fmaf(a0 - am1, c9, -((ap1 - am2) * c24));
+}
+// Forward-staggered difference at k: 9(ap1 - a0)/(8h) - (ap2 - am1)/(24h).
+__device__ __forceinline__ float st_dplus(float ap1, float a0, float ap2, float am1, float c9, float c24) {
+    return fmaf(ap1 - a0, c9, -((ap2 - am1) * c24));
+}
+// v' = ab (v + dt ds / rho)   (updateV*, solver/fdm.h:150-161)
+__device__ __forceinline__ float st_velocity(float ab, float dt, float ds, float rinv, float v) {
+    return ab * fmaf(dt * ds, rinv, v);
+}
+// u' = u + v' dt
+__device__ __forceinline__ float st_displacement(float u, float vn, float dt) { return fmaf(vn, dt, u); }
+// P-SV stress update (updateSXZ, solver/fdm.h:143-149).
+__device__ __forceinline__ void st_stress_psv(float &sxx, float &szz, float &sxz, float l, float m, float dt,
+                                              float dvxdx, float dvxdz, float dvzdx, float dvzdz) {
+    const float l2m = fmaf(2.f, m, l);
+    sxx = fmaf(dt, fmaf(l2m, dvxdx, l * dvzdz), sxx);
+    szz = fmaf(dt, fmaf(l2m, dvzdz, l * dvxdx), szz);
+    sxz = fmaf(dt, m * (dvxdz + dvzdx), sxz);
+}
+// SH stress update (updateSY, solver/fdm.h:138-142).
+__device__ __forceinline__ void st_stress_sh(float &sxy, float &szy, float m, float dt, float dvydx, float dvydz) {
+    const float dtm = dt * m;
+    sxy = fmaf(dtm, dvydx, sxy);
+    szy = fmaf(dtm, dvydz, szy);
+}
+
+}  // namespace gb

@@ -26,18 +26,17 @@
 #include <cuda_fp16.h>
 
 #include "gb_internal.h"
+#include "gb_stencil.h"
 
 namespace gb {
 
 constexpr int kThreads = 256;
 
-// Backward-staggered difference at k: 9(a0 - am1)/(8h) - (ap1 - am2)/(24h).
 __device__ __forceinline__ float dminus(float a0, float am1, float ap1, float am2, float c9, float c24) {
-    return fmaf(a0 - am1, c9, -((ap1 - am2) * c24));
+    return st_dminus(a0, am1, ap1, am2, c9, c24);
 }
-// Forward-staggered difference at k: 9(ap1 - a0)/(8h) - (ap2 - am1)/(24h).
 __device__ __forceinline__ float dplus(float ap1, float a0, float ap2, float am1, float c9, float c24) {
-    return fmaf(ap1 - a0, c9, -((ap2 - am1) * c24));
+    return st_dplus(ap1, a0, ap2, am1, c9, c24);
 }
 
 struct Csr {
@@ -264,11 +263,11 @@ __global__ void __launch_bounds__(kThreads) k_step(const Slot *__restrict__ slot
         const bool own = c >= 1 && c <= TX && r >= 1 && r <= TZ;
 #pragma unroll
         for (int f = 0; f < NV; f++) {
-            const float vn = ab * fmaf(dt * ds[f], rinv, s_v[f][e]);
+            const float vn = st_velocity(ab, dt, ds[f], rinv, s_v[f][e]);
             s_v[f][e] = vn;
             if (own) {
                 v_out[f][k] = vn;
-                u[f][k] = u_reg[q][f] + vn * dt;
+                u[f][k] = st_displacement(u_reg[q][f], vn, dt);
             }
         }
     }
@@ -321,17 +320,19 @@ __global__ void __launch_bounds__(kThreads) k_step(const Slot *__restrict__ slot
                 dvxdz = dplus(VV(0, 0, 1), VV(0, 0, 0), VV(0, 0, 2), VV(0, 0, -1), c9z, c24z);
                 dvzdz = dplus(VV(1, 0, 1), VV(1, 0, 0), VV(1, 0, 2), VV(1, 0, -1), c9z, c24z);
             }
-            const float l = lam_reg[q];
-            const float l2m = l + 2.f * m;
-            sig_out[0][k] = s_sig[0][se] + dt * (l2m * dvxdx + l * dvzdz);
-            sig_out[1][k] = s_sig[1][se] + dt * (l2m * dvzdz + l * dvxdx);
-            sig_out[2][k] = s_sig[2][se] + dt * (m * (dvxdz + dvzdx));
+            float sxx = s_sig[0][se], szz = s_sig[1][se], sxz = s_sig[2][se];
+            st_stress_psv(sxx, szz, sxz, lam_reg[q], m, dt, dvxdx, dvxdz, dvzdx, dvzdz);
+            sig_out[0][k] = sxx;
+            sig_out[1][k] = szz;
+            sig_out[2][k] = sxz;
         } else {
             float dvydx = 0.f, dvydz = 0.f;
             if (i >= 1 && i < nx - 2) dvydx = dplus(VV(0, 1, 0), VV(0, 0, 0), VV(0, 2, 0), VV(0, -1, 0), c9x, c24x);
             if (j >= 1 && j < nz - 2) dvydz = dplus(VV(0, 0, 1), VV(0, 0, 0), VV(0, 0, 2), VV(0, 0, -1), c9z, c24z);
-            sig_out[0][k] = s_sig[0][se] + dt * m * dvydx;
-            sig_out[1][k] = s_sig[1][se] + dt * m * dvydz;
+            float sxy = s_sig[0][se], szy = s_sig[1][se];
+            st_stress_sh(sxy, szy, m, dt, dvydx, dvydz);
+            sig_out[0][k] = sxy;
+            sig_out[1][k] = szy;
         }
 #undef VV
     }
@@ -370,14 +371,7 @@ cudaError_t launch_step(bool psv, TileCfg tc, const Slot *d_slots, int nslots, i
 // it, into slot isfe = nsfe - (it+1)/sfe. Storage is FP32, BF16 or FP16; the
 // 16-bit forms use one power-of-two scale per snapshot and field, derived
 // from the field's max |value|, so the scaling itself adds no rounding.
-__device__ __forceinline__ float ckpt_scale(float amax, int prec) {
-    if (!(amax > 0.f) || prec == CKPT_F32) return 1.f;
-    // FP16: map amax to at most 2^15 (fp16 max 65504); BF16: to at most 1.
-    const float target = prec == CKPT_F16 ? 32768.f : 1.f;
-    int e;
-    frexpf(target / amax, &e);  // target/amax = m * 2^e, m in [0.5, 1)
-    return ldexpf(1.f, e - 1);  // largest power of two <= target/amax
-}
+__device__ __forceinline__ float ckpt_scale(float amax, int prec) { return ckpt_scale_of(amax, prec); }
 
 // Fields of one checkpoint group: q index in the slot's checkpoint and the
 // state array that feeds it.

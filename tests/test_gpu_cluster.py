@@ -1,0 +1,76 @@
+"""Cluster-resident passes (a whole forward or adjoint pass per shot inside
+one thread-block cluster, state in distributed shared memory) against the
+per-step kernels and the CPU oracle."""
+import numpy as np
+import pytest
+
+from tests import cases
+
+pytestmark = pytest.mark.gpu
+
+
+def comps(wave):
+    return "xz" if wave == "psv" else "y"
+
+
+def names(wave):
+    return ("k_lambda", "k_mu", "k_rho") if wave == "psv" else ("k_mu", "k_rho")
+
+
+def run(gpu, case, cluster, ad):
+    cfg, sol = cases.gpu_solver(gpu, case)
+    sol.set_option("cluster", cluster)
+    shots = list(range(case["nsrc"]))
+    sol.run_forward_batch(shots)
+    tr = [{c: sol.out(c, slot=b) for c in comps(case["wave"])} for b in shots]
+    st = sol.stats()
+    for b in shots:
+        for c in comps(case["wave"]):
+            sol.set_adstf(c, ad[b][c], slot=b)
+    sol.initKernels()
+    sol.run_adjoint_batch(shots)
+    return tr, sol.kernels(), st
+
+
+@pytest.mark.parametrize("wave,nx,nz,nt", [("sh", 681, 141, 400), ("psv", 200, 200, 300), ("sh", 97, 61, 300),
+                                           ("psv", 150, 110, 300)])
+def test_cluster_pass_matches_step_kernels(gpu, orc, wave, nx, nz, nt):
+    case = cases.make_case(wave=wave, nx=nx, nz=nz, nt=nt, nsrc=3, nrec=min(nx - 4, 60), sfe=10, seed=nx)
+    rng = np.random.default_rng(nz)
+    ad = [{c: (rng.standard_normal((case["nrec"], nt)) * 1e-3).astype(np.float32) for c in "xyz"}
+          for _ in range(3)]
+    tr_c, k_c, st_c = run(gpu, case, 1, ad)
+    tr_t, k_t, st_t = run(gpu, case, 0, ad)
+    assert st_c.tile_tz < 0, "the cluster path did not run"
+    assert st_t.tile_tz > 0
+    for b in range(3):
+        for c in comps(wave):
+            np.testing.assert_array_equal(tr_c[b][c], tr_t[b][c])
+    for n in names(wave):
+        # the cluster pass sums each shot's contribution separately
+        assert cases.rel(k_c[n], k_t[n]) < 1e-6, n
+
+
+def test_cluster_adjoint_matches_oracle(gpu, orc):
+    case = cases.make_case(wave="psv", nx=120, nz=96, nt=400, nsrc=2, nrec=40, sfe=10, seed=11)
+    pb = cases.oracle_problem(orc, case)
+    rng = np.random.default_rng(2)
+    ad = [{c: (rng.standard_normal((pb.nrec, pb.nt)) * 1e-3).astype(np.float32) for c in "xyz"} for _ in range(2)]
+    tr, k, st = run(gpu, case, 1, ad)
+    assert st.tile_tz < 0
+    kern = None
+    for s in range(2):
+        o = orc.forward(pb, s, adj=True)
+        for c in "xz":
+            assert cases.rel(tr[s][c], o["xyz".index(c)]) < 1e-5
+        kern = orc.adjoint(pb, [ad[s]["x"], ad[s]["y"], ad[s]["z"]], o[3], kern)
+    for q, n in enumerate(("k_lambda", "k_mu", "k_rho")):
+        assert cases.rel(k[n], kern[q]) < 1e-4, n
+
+
+def test_cluster_falls_back_for_16bit_checkpoints(gpu, orc):
+    case = cases.make_case(wave="sh", nx=100, nz=60, nt=200, nsrc=1, nrec=20, seed=3)
+    cfg, sol = cases.gpu_solver(gpu, case)
+    sol.set_option("ckpt", 2)
+    sol.run_forward_batch([0])
+    assert sol.stats().tile_tz > 0

@@ -106,6 +106,7 @@ def test_kernel_configurations_give_identical_results(gpu, orc, tile, wave):
 
     def run(t):
         cfg, sol = cases.gpu_solver(gpu, case)
+        sol.set_option("cluster", 0)
         sol.set_option("tile", t)
         sol.run_forward_batch([0, 1])
         tr = {c: sol.out(c, slot=1) for c in comps(wave)}
@@ -128,8 +129,10 @@ def test_graphs_and_eager_identical(gpu, orc):
     case = cases.make_case(wave="sh", nx=100, nz=64, nt=300, nsrc=2, nrec=20, seed=19)
     cfg, a = cases.gpu_solver(gpu, case)
     a.set_option("graphs", 0)
+    a.set_option("cluster", 0)
     cfg2, b = cases.gpu_solver(gpu, case)
     b.set_option("graphs", 1)
+    b.set_option("cluster", 0)
     for s in range(2):
         a.runForward(s)
         b.runForward(s)
