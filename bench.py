@@ -178,8 +178,8 @@ def peaks():
 
 
 def profiled_traffic(kernel_tag):
-    """DRAM bytes per launch of the step kernel from the committed ncu
-    summary (profiles/dram_traffic.txt: `<tag> <bytes per launch> <note>`)."""
+    """DRAM bytes per time step of the dominant kernel from the committed ncu
+    summary (profiles/dram_traffic.txt: `<tag> <bytes per step> <note>`)."""
     p = os.path.join(ROOT, "profiles", "dram_traffic.txt")
     if not os.path.exists(p):
         return None
@@ -284,17 +284,32 @@ def run_ours(args, ws, rank, local):
     value = NSHOT * args.steps * ws / (total_ms / 1e3)
     cells = NX * NZ
 
-    # roofline of the fused step kernel (SH: 40 algorithmic bytes per cell-update)
+    # Roofline of the dominant kernel. The algorithmic bytes of one SH time
+    # step are those of the per-step formulation: 40 bytes per cell (v, u,
+    # two stresses read and written, mu and 1/rho read) for every shot.
+    # step_ms / step_launches is the time per step (a cluster-resident pass
+    # books its duration as nt steps).
     per_launch_ms = st.step_ms / max(st.step_launches, 1)
     algo_bytes = 40.0 * cells * NSHOT
     achieved = algo_bytes / (per_launch_ms * 1e-3) / 1e9
     peak, peak_kind = peaks()
+    clustered = st.tile_tz < 0
+    if clustered:
+        kname = "k_cluster<SH> (whole forward/adjoint pass per shot in a %d-CTA cluster, state in shared memory)" % (
+            -st.tile_tz)
+        tag = "cluster_sh_c2"
+        note = ("the wavefield stays in shared memory for the whole pass: DRAM traffic per step (traffic) is the "
+                "checkpoints and traces only, far below the algorithmic bytes; achieved/peak compares the step "
+                "time with an HBM-bound per-step kernel at the measured copy bandwidth")
+    else:
+        kname = "k_step<SH> (fused velocity+stress step, 16 shots per launch)"
+        tag = "step_sh_c2"
+        note = "state (16 shots x 4 fields + model) is L2-resident at this size"
     roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-            "frac": round(achieved / peak, 3), "traffic": profiled_traffic("step_sh_c2"),
-            "kernel": "k_step<SH> (fused velocity+stress step, 16 shots per launch)",
-            "algorithmic_bytes_per_launch": algo_bytes, "avg_launch_us": round(per_launch_ms * 1e3, 2),
+            "frac": round(achieved / peak, 3), "traffic": profiled_traffic(tag),
+            "kernel": kname, "algorithmic_bytes_per_step": algo_bytes, "avg_step_us": round(per_launch_ms * 1e3, 2),
             "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
-            "note": "state (16 shots x 4 fields + model) is L2-resident at this size; see profiles/"}
+            "note": note}
 
     # end to end through the C ABI with pinned host buffers
     n_obs = obs.size
@@ -324,10 +339,11 @@ def run_ours(args, ws, rank, local):
     # plain path: one shot per launch sequence, no graphs (same GPU, one gradient)
     plain = None
     if rank == 0 and not args.no_plain:
-        cfgp = pkg.Config.new(tmp, dict(wl["values"], batch=1, graphs=0), wl["src"], wl["rec"])
+        cfgp = pkg.Config.new(tmp, dict(wl["values"], batch=1, graphs=0, cluster=0), wl["src"], wl["rec"])
         sp = pkg.FdmSolver(cfgp, grid=(NX, NZ, wl["xmax"], wl["zmax"]))
         sp.set_option("batch", 1)
         sp.set_option("graphs", 0)
+        sp.set_option("cluster", 0)
         sp.set_model_grid(*wl["init"])
         mp = pkg.Misfit.from_obs(1, sp, {"y": obs}, pkg.GaussianFilter(NX, NZ, SIGMA))
         mp.run(kernel=True)
@@ -335,7 +351,7 @@ def run_ours(args, ws, rank, local):
         mp.run(kernel=True)
         plain_ms = sp.timer_end()
         plain = {"value": round(NSHOT / (plain_ms / 1e3), 3), "unit": "shots/s", "ms_per_step": round(plain_ms, 2),
-                 "what": "batch 1, no CUDA graphs, same kernels"}
+                 "what": "one shot per call, one fused step kernel launch per time step, no CUDA graphs"}
         mp.close()
         sp.close()
 
@@ -592,8 +608,9 @@ def run_profile_case(args):
     cfg, sol = cases.gpu_solver(pkg, case)
     sol.set_option("tile", args.tile)
     sol.set_option("graphs", 0)
+    sol.set_option("cluster", args.cluster)
     sol.run_forward_batch(list(range(case["nsrc"])))
-    print("profile case", name, "tile", args.tile, "done")
+    print("profile case", name, "tile", args.tile, "cluster", args.cluster, "done")
 
 
 def run_reference(args, ws, rank):
@@ -660,6 +677,8 @@ def main():
     ap.add_argument("--sequential", type=int, default=64, help="c4 requests also solved one at a time")
     ap.add_argument("--profile-case", default="", help="run one small case for an ncu capture")
     ap.add_argument("--tile", type=int, default=3, help="kernel configuration for --profile-case")
+    ap.add_argument("--cluster", type=int, default=0,
+                    help="--profile-case: 0 per-step kernels, 1 cluster-resident (automatic size), 2..16 that size")
     args = ap.parse_args()
     if args.profile_case:
         run_profile_case(args)

@@ -136,7 +136,8 @@ int gb_solver_batch_capacity(gb_solver *s);
 /* Runtime options: "batch" (slots, 0 = from the HBM budget), "graphs" (0/1),
  * "ckpt" (0 FP32, 1 BF16, 2 FP16), "tile" (0 autotune, 1..20 fixed),
  * "cluster" (1: run whole passes in thread-block clusters when a shot's
- * state fits in their shared memory, 0: never), "hbm_budget_gb". Options
+ * state fits in their shared memory, with the cluster size chosen by
+ * occupancy; 2..16: that cluster size; 0: never), "hbm_budget_gb". Options
  * change no forward result; "ckpt" changes kernels by the checkpoint
  * rounding and "cluster" by the order in which shots are summed. */
 int gb_solver_set_option(gb_solver *s, const char *key, double value);

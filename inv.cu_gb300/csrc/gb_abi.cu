@@ -303,7 +303,9 @@ int gb_solver_set_option(gb_solver *s, const char *key, double value) {
         if (t == 0) v.tile_id = 0;
         v.invalidate_graphs();
     } else if (k == "cluster") {
-        v.opt_cluster = value != 0;
+        const int c = (int)value;
+        if (c < 0 || c > 16) return GB_ERR_ARG;
+        v.opt_cluster = c;
     } else if (k == "hbm_budget_gb") {
         if (v.capacity) {
             set_error("option hbm_budget_gb: set it before the first run");

@@ -1,25 +1,31 @@
 // Cluster-resident solver: a whole forward or adjoint pass of one shot in one
-// thread-block cluster, with the wavefield kept in distributed shared memory.
+// thread-block cluster, with the wavefield kept in shared memory.
 //
 // When a shot's state (P-SV 7 fields, SH 4 fields, FP32) fits in the shared
 // memory of R CTAs (R <= 16), the time loop runs inside one persistent
-// kernel: CTA r of a cluster owns the grid columns [r*cp, (r+1)*cp) and keeps
-// their state in its shared memory; the x-neighbours of its first and last
-// columns are read from the neighbouring CTAs' shared memory through the
-// cluster (distributed shared memory). Each time step is
+// kernel. CTA r of a cluster owns the grid columns [r*cp, r*cp + ncols) and
+// keeps them in its shared memory, with two ghost columns on either side.
+// Each thread owns one grid row of up to QM consecutive columns and keeps the
+// model of those cells (1/rho, mu, lambda) in registers for the whole pass;
+// the x damping profile and the CTA's receiver ids sit in small shared
+// tables behind the fields. Each time step is
 //   phase A  stress divergence, sources, velocity and displacement update
 //   barrier  (all velocities written, all stresses of step n still in place)
 //   phase B  velocity gradients and stress update
 //   barrier  (all stresses written before the next phase A reads them)
 // plus, in the adjoint, the kernel accumulation every sfe steps (one more
-// barrier). Only receivers, checkpoints and the model (read from L2) touch
-// memory outside the SM, so the per-step cost is the stencil arithmetic and
-// shared-memory traffic instead of DRAM/L2 round trips and kernel launches.
+// barrier). A thread that updates one of the CTA's edge columns also writes
+// the new value into the neighbouring CTA's ghost column (st.shared::cluster,
+// made visible by the cluster barrier's release/acquire), so the stencils
+// only ever read the CTA's own shared memory. The x-differences walk the
+// thread's columns with a sliding window: one new shared-memory load per
+// field per cell.
 //
 // Every cell is computed with the operations, in the order, of the fused
-// step kernels (gb_step.cu): forward traces and checkpoints are bit-identical
-// to theirs. The adjoint accumulates each shot's kernel contribution in a
-// per-shot buffer that is added to the kernels after the pass, in shot order.
+// step kernels (gb_stencil.h): forward traces and checkpoints are
+// bit-identical to theirs. The adjoint accumulates each shot's kernel
+// contribution in a per-shot buffer that is added to the kernels after the
+// pass, in shot order.
 #include <cooperative_groups.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -33,12 +39,34 @@ namespace cg = cooperative_groups;
 
 namespace gb {
 
-__device__ __forceinline__ float cdm(float a0, float am1, float ap1, float am2, float c9, float c24) {
-    return st_dminus(a0, am1, ap1, am2, c9, c24);
+// Threads per CTA for QM columns per thread: the model registers (2 per
+// owned cell for SH, 3 for P-SV) plus about 56 (SH) or 64 (P-SV) registers of
+// per-thread state must fit in the 65536-register file of the SM.
+__host__ __device__ constexpr int cluster_threads_for(bool psv, int qm) {
+    return psv ? (qm <= 4 ? 800 : qm <= 8 ? 736 : qm <= 12 ? 608 : qm <= 16 ? 576 : 480)
+               : (qm <= 4 ? 1024 : qm <= 8 ? 896 : qm <= 12 ? 800 : qm <= 16 ? 736 : 608);
 }
-__device__ __forceinline__ float cdp(float ap1, float a0, float ap2, float am1, float c9, float c24) {
-    return st_dplus(ap1, a0, ap2, am1, c9, c24);
+
+int cluster_max_threads(bool psv, int qm) { return cluster_threads_for(psv, qm); }
+
+// Row stride of a shared-memory field: cp + 4 columns, made odd.
+__host__ __device__ inline int cluster_row_stride(int cp) { return (cp + 4) | 1; }
+
+__device__ __forceinline__ uint32_t cl_mapa(uint32_t addr, uint32_t rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+    return r;
 }
+__device__ __forceinline__ void cl_st(uint32_t addr, float v) {
+    asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(addr), "f"(v) : "memory");
+}
+
+// 4-byte asynchronous copy global -> shared (completed by cp_async_wait_all)
+__device__ __forceinline__ void cp_async4(float *dst, const float *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 __device__ __forceinline__ float ck_get(const Slot &S, int isfe, int q, size_t k, size_t n, float inv) {
     const size_t off = ((size_t)isfe * S.nf + q) * n + k;
@@ -48,179 +76,316 @@ __device__ __forceinline__ float ck_get(const Slot &S, int isfe, int q, size_t k
 }
 
 // Shared-memory field order. P-SV: vx vz ux uz sxx szz sxz; SH: vy uy sxy szy.
-template <bool PSV, bool ADJ>
-__global__ void __launch_bounds__(1024, 1) k_cluster(const Slot *__restrict__ slots, ClusterGeom g,
-                                                     float *__restrict__ kpart) {
-    constexpr int NF = PSV ? 7 : 4;
+// Each field is stored by rows (x fastest) with two zero pad rows above and
+// below it: field f, row j (-2 .. nz+1), local column c (-2 .. cp+1) at
+// sm[f*fs + (j+2)*rs + c + 2], fs = (nz+4)*rs. The row stride rs >= cp + 4 is
+// odd, so that a warp of consecutive rows hits 32 distinct banks, and a
+// thread's consecutive columns are immediate offsets from one address.
+//
+// cp is a multiple of QM and every thread updates QM columns; in the last CTA
+// the columns past the grid are updated too (never read by a grid column:
+// the x differences of the last two grid columns are masked off).
+template <bool PSV, bool ADJ, int QM>
+__global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
+    k_cluster(const Slot *__restrict__ slots, ClusterGeom g, float *__restrict__ kpart) {
     constexpr int NV = PSV ? 2 : 1;
+    constexpr int NF = PSV ? 7 : 4;
+    constexpr int NSF = NF - 2 * NV;             // stress fields
     constexpr int FV = 0, FU = NV, FS = 2 * NV;  // first velocity, displacement, stress field
+    constexpr int NWA = PSV ? 2 : 1;             // stresses differentiated in x in phase A
     extern __shared__ float sm[];
     cg::cluster_group cl = cg::this_cluster();
+    const int R = g.R;
     const int rank = (int)cl.block_rank();
-    const int slot = blockIdx.x / g.R;
+    const int slot = blockIdx.x / R;
     const Slot &S = slots[slot];
     if (!S.active) return;  // uniform over the cluster: one slot per cluster
-    const int nx = S.nx, nz = S.nz, nt = S.nt, cp = g.cols_per;
+    const int nx = g.nx, nz = g.nz, nt = g.nt, cp = g.cols_per;
     const size_t ncell = (size_t)nx * nz;
-    const int x0 = rank * cp, x1 = min(x0 + cp, nx);
-    const int t = threadIdx.x, row = t % g.rows_pad, grp = t / g.rows_pad;
-    const bool act = row < nz && grp < g.G;
-    const int ncol = (act && x1 - x0 > grp) ? (x1 - x0 - grp + g.G - 1) / g.G : 0;
+    const int x0 = rank * cp;
+    const int ncols = min(cp, nx - x0);  // grid columns of this CTA, >= 2
+    const int rs = cluster_row_stride(cp);
+    const int fs = (nz + 4) * rs;  // one field
+    const int t = threadIdx.x, j = t % nz, grp = t / nz;
+    const int cb = grp * QM;                     // first local column of this thread
+    const int nq = max(0, min(QM, ncols - cb));  // of which grid columns
+    const int i0 = x0 + cb;                      // its global column
 
-    // shared memory: NF fields [cp][nz], then the receiver map [cp][nz] (the
-    // receiver, or adjoint source, at each owned cell; -1 for none)
-    int *recmap = reinterpret_cast<int *>(sm + (size_t)NF * cp * nz);
-    for (int e = t; e < NF * cp * nz; e += blockDim.x) sm[e] = 0.f;
-    for (int e = t; e < cp * nz; e += blockDim.x) recmap[e] = -1;
+    // receiver (or adjoint source) of each owned cell, through a map built in
+    // the still unused field memory; the ids of the thread's receivers go to
+    // rtab[rbase ...] in column order
+    float *s_ax = sm + NF * fs;                          // ax of columns -2 .. cp+1
+    int *rtab = reinterpret_cast<int *>(s_ax + cp + 4);  // g.nrec_cta entries
+    // per receiver entry NV values: the samples recorded in phase A (forward)
+    // or the next step's adjoint source (adjoint); then NV values of the next
+    // step's forward source
+    float *rbuf = reinterpret_cast<float *>(rtab + g.nrec_cta);
+    float *sbuf = rbuf + (size_t)g.nrec_cta * NV;
+    __shared__ int s_count;
+    int *map = reinterpret_cast<int *>(sm);
+    for (int e = t; e < cp * nz; e += blockDim.x) map[e] = -1;
+    if (t == 0) s_count = 0;
     __syncthreads();
     for (int r = t; r < S.npts; r += blockDim.x) {
-        const int i = S.pts_i[r], j = S.pts_j[r];
-        if (i >= x0 && i < x1 && j >= 0 && j < nz) recmap[(i - x0) * nz + j] = r;  // cells are distinct
+        const int i = S.pts_i[r] - x0, jj = S.pts_j[r];
+        if (i >= 0 && i < ncols && jj >= 0 && jj < nz) map[i * nz + jj] = r;  // cells are distinct
     }
-    const int src_k = (!ADJ && S.src_trace >= 0) ? S.src_i * nz + S.src_j : -1;  // forward source cell
-
-    const float dt = S.dt, c9x = S.c9x, c24x = S.c24x, c9z = S.c9z, c24z = S.c24z;
-    const float azj = act ? __ldg(S.az + row) : 0.f;
-    const bool zS = row >= 2 && row < nz - 2, zV = row >= 1 && row < nz - 2;
-    const int base_ck = (PSV && S.sh[0] != nullptr) ? 2 : 0;  // checkpoint field offset of this system
-    cl.sync();
-
-    // column i of field f: own shared memory or a neighbour's, by rank
-    auto col = [&](int f, int i) -> const float * {
-        const int owner = i / cp;
-        float *p = sm + ((size_t)f * cp + (i - owner * cp)) * nz;
-        return owner == rank ? p : cl.map_shared_rank(p, owner);
-    };
-    auto own = [&](int f, int i) -> float * { return sm + ((size_t)f * cp + (i - x0)) * nz; };
-
-    for (int it = 0; it < nt; it++) {
-        // forward checkpoint of displacement before the step
-        int isfe = -1;
-        if (!ADJ && S.ckpt && S.sfe > 0 && (it + 1) % S.sfe == 0) isfe = S.nsfe - (it + 1) / S.sfe;
-        if (isfe >= 0) {
-            for (int q = 0; q < ncol; q++) {
-                const int i = x0 + grp + q * g.G;
-                const size_t k = (size_t)i * nz + row;
+    __syncthreads();
+    unsigned rmask = 0, xs_mask = 0, xv_mask = 0;
 #pragma unroll
-                for (int f = 0; f < NV; f++)
-                    static_cast<float *>(S.ckpt)[((size_t)isfe * S.nf + base_ck + f) * ncell + k] = own(FU + f, i)[row];
+    for (int q = 0; q < QM; q++) {
+        if (q < nq && map[(cb + q) * nz + j] >= 0) rmask |= 1u << q;
+        const int i = i0 + q;
+        if (i >= 2 && i < nx - 2) xs_mask |= 1u << q;
+        if (i >= 1 && i < nx - 2) xv_mask |= 1u << q;
+    }
+    const int rbase = rmask ? atomicAdd(&s_count, __popc(rmask)) : 0;
+    if (rbase + __popc(rmask) > g.nrec_cta) rmask = 0;  // not reached: the host sizes the table
+    {
+        int n = 0;
+#pragma unroll
+        for (int q = 0; q < QM; q++)
+            if ((rmask >> q) & 1) rtab[rbase + n++] = map[(cb + q) * nz + j];
+    }
+    int srcq = -1;  // owned column of the forward source
+    if (!ADJ && S.src_trace >= 0 && S.src_j == j && S.src_i - i0 >= 0 && S.src_i - i0 < nq) srcq = S.src_i - i0;
+    // cells that inject or record
+    const unsigned spmask = rmask | (srcq >= 0 ? 1u << srcq : 0u);
+    __syncthreads();
+    for (int e = t; e < NF * fs; e += blockDim.x) sm[e] = 0.f;
+    for (int c = t - 2; c < cp + 2; c += blockDim.x) s_ax[c + 2] = __ldg(S.ax + min(max(x0 + c, 0), nx - 1));
+
+    // model of the owned cells
+    float p_ri[QM], p_mu[QM], p_la[PSV ? QM : 1];
+    const float azj = __ldg(S.az + j);
+#pragma unroll
+    for (int q = 0; q < QM; q++) {
+        const int i = min(i0 + q, nx - 1);  // columns past the grid use the last one's
+        const size_t k = (size_t)i * nz + j;
+        p_ri[q] = __ldg(S.rinv + k);
+        p_mu[q] = __ldg(S.mu + k);
+        if (PSV) p_la[q] = __ldg(S.lambda + k);
+    }
+
+    const float dt = g.dt, c9x = g.c9x, c24x = g.c24x, c9z = g.c9z, c24z = g.c24z;
+    const bool zS = j >= 2 && j < nz - 2, zV = j >= 1 && j < nz - 2;
+    const int base_ck = (PSV && S.sh[0] != nullptr) ? 2 : 0;  // checkpoint field offset of this system
+    float *const P = sm + (j + 2) * rs + cb + 2;             // field 0, row j, column cb
+    // neighbours' shared memory: cluster address of their field 0, row j, column -2
+    const uint32_t me = (uint32_t)__cvta_generic_to_shared(sm + (j + 2) * rs);
+    const uint32_t lf = rank > 0 ? cl_mapa(me, rank - 1) : 0u;
+    const uint32_t rt = rank < R - 1 ? cl_mapa(me, rank + 1) : 0u;
+    // the thread owning columns 0, 1 sends them left; the one owning columns
+    // cp-2, cp-1 sends them right (a CTA with a right neighbour holds cp columns)
+    const bool edge_l = rank > 0 && grp == 0, edge_r = rank < R - 1 && cb + QM == cp;
+    const int nrq = __popc(rmask);
+
+    // checkpoint index written after step `step` (-1: none)
+    auto ckpt_of = [&](int step) -> int {
+        if (ADJ || !S.ckpt || S.sfe <= 0 || (step + 1) % S.sfe != 0) return -1;
+        return S.nsfe - (step + 1) / S.sfe;
+    };
+    // owned grid cells of NV fields from field f0 to checkpoint field q0
+    auto store_ckpt = [&](int isfe, int f0, int q0) {
+        float *ck = static_cast<float *>(S.ckpt) + ((size_t)isfe * S.nf + base_ck + q0) * ncell + (size_t)i0 * nz + j;
+#pragma unroll 1
+        for (int q = 0; q < nq; q++)
+#pragma unroll
+            for (int f = 0; f < NV; f++) ck[f * ncell + (size_t)q * nz] = P[(f0 + f) * fs + q];
+    };
+    auto inj_of = [&](int f) -> const float * { return PSV ? (f == 0 ? S.inj_x : S.inj_z) : S.inj_y; };
+    // injection of step `step` into shared memory, read after cp_async_wait_all
+    auto prefetch = [&](int step) {
+        if (step >= nt) return;
+        if (!ADJ && srcq >= 0) {
+#pragma unroll
+            for (int f = 0; f < NV; f++) cp_async4(sbuf + f, inj_of(f) + (size_t)S.src_trace * nt + step);
+        }
+        if (ADJ) {
+#pragma unroll 1
+            for (int n = 0; n < nrq; n++) {
+                const int e = rbase + n;
+                const size_t ks = (size_t)rtab[e] * nt + step;
+#pragma unroll
+                for (int f = 0; f < NV; f++) cp_async4(rbuf + e * NV + f, inj_of(f) + ks);
             }
         }
+    };
+    cl.sync();
+    if (ckpt_of(0) >= 0) store_ckpt(ckpt_of(0), FU, 0);  // displacement before step 0
+    prefetch(0);
+
+    unsigned rb = (unsigned)rbase, sq = (unsigned)srcq, qn = (unsigned)nq;
+    unsigned fl = (edge_l ? 1u : 0u) | (edge_r ? 2u : 0u) | (zS ? 4u : 0u) | (zV ? 8u : 0u);
+    unsigned spm = spmask;
+    for (int it = 0; it < nt; it++) {
+        // The per-column conditions below are invariant over the time loop;
+        // hoisting them out of it would hold registers per owned column.
+        // Redefining their inputs each step keeps them local.
+        asm volatile("" : "+r"(xs_mask), "+r"(xv_mask), "+r"(rmask), "+r"(rb));
+        asm volatile("" : "+r"(sq), "+r"(qn), "+r"(fl), "+r"(spm));
+        const int nq = (int)qn, srcq = (int)sq, rbase = (int)rb;
+        const bool eL = fl & 1u, eR = fl & 2u, zs = fl & 4u, zv = fl & 8u;
+        if (spm) cp_async_wait_all();  // this step's injection
         // ---- phase A: divergence, sources, velocity, displacement
-        for (int q = 0; q < ncol; q++) {
-            const int i = x0 + grp + q * g.G;
-            const size_t k = (size_t)i * nz + row;
-            const bool xS = i >= 2 && i < nx - 2;
-            float ds[NV];
-            const bool inner = i - 2 >= x0 && i + 1 < x1;
-            if (PSV) {
-                // sxx (x), sxz (x and z), szz (z)
-                const float *a0 = own(FS + 0, i), *c0 = own(FS + 2, i), *b0 = own(FS + 1, i);
-                float dsx = 0.f, dsz = 0.f;
-                if (xS) {
-                    const float *am1 = inner ? a0 - nz : col(FS + 0, i - 1), *ap1 = inner ? a0 + nz : col(FS + 0, i + 1),
-                                *am2 = inner ? a0 - 2 * nz : col(FS + 0, i - 2);
-                    const float *cm1 = inner ? c0 - nz : col(FS + 2, i - 1), *cp1 = inner ? c0 + nz : col(FS + 2, i + 1),
-                                *cm2 = inner ? c0 - 2 * nz : col(FS + 2, i - 2);
-                    dsx = cdm(a0[row], am1[row], ap1[row], am2[row], c9x, c24x);
-                    dsz = cdm(c0[row], cm1[row], cp1[row], cm2[row], c9x, c24x);
-                }
-                if (zS) {
-                    dsx += cdm(c0[row], c0[row - 1], c0[row + 1], c0[row - 2], c9z, c24z);
-                    dsz += cdm(b0[row], b0[row - 1], b0[row + 1], b0[row - 2], c9z, c24z);
-                }
-                ds[0] = dsx;
-                ds[NV - 1] = dsz;
-            } else {
-                const float *a0 = own(FS + 0, i), *b0 = own(FS + 1, i);
-                float dsy = 0.f;
-                if (xS) {
-                    const float *am1 = inner ? a0 - nz : col(FS + 0, i - 1), *ap1 = inner ? a0 + nz : col(FS + 0, i + 1),
-                                *am2 = inner ? a0 - 2 * nz : col(FS + 0, i - 2);
-                    dsy = cdm(a0[row], am1[row], ap1[row], am2[row], c9x, c24x);
-                }
-                if (zS) dsy += cdm(b0[row], b0[row - 1], b0[row + 1], b0[row - 2], c9z, c24z);
-                ds[0] = dsy;
-            }
-            const int rq = recmap[(i - x0) * nz + row];
-            if (!ADJ && (int)k == src_k) {
-                const size_t ks = (size_t)S.src_trace * nt + it;
-                if (PSV) {
-                    ds[0] += __ldg(S.inj_x + ks);
-                    ds[NV - 1] += __ldg(S.inj_z + ks);
-                } else {
-                    ds[0] += __ldg(S.inj_y + ks);
-                }
-            }
-            if (ADJ && rq >= 0) {
-                const size_t ks = (size_t)rq * nt + it;
-                if (PSV) {
-                    ds[0] += __ldg(S.inj_x + ks);
-                    ds[NV - 1] += __ldg(S.inj_z + ks);
-                } else {
-                    ds[0] += __ldg(S.inj_y + ks);
-                }
-            }
-            const float ab = __ldg(S.ax + i) * azj;
-            const float rinv = __ldg(S.rinv + k);
-            float vn[NV], un[NV];
+        {
+            float wa[NWA][4];  // x-window: columns c-2, c-1, c, c+1
 #pragma unroll
-            for (int f = 0; f < NV; f++) {
-                float *pv = own(FV + f, i), *pu = own(FU + f, i);
-                vn[f] = st_velocity(ab, dt, ds[f], rinv, pv[row]);
-                un[f] = st_displacement(pu[row], vn[f], dt);
-                pv[row] = vn[f];
-                pu[row] = un[f];
+            for (int w = 0; w < NWA; w++) {
+                const float *p = P + (FS + 2 * w) * fs;
+                wa[w][0] = p[-2];
+                wa[w][1] = p[-1];
+                wa[w][2] = p[0];
             }
-            if (!ADJ && rq >= 0) {
-                const size_t kr = (size_t)rq * nt + it;
-                if (PSV) {
-                    S.out_x[kr] = S.record_u ? un[0] : vn[0];
-                    S.out_z[kr] = S.record_u ? un[NV - 1] : vn[NV - 1];
-                } else {
-                    S.out_y[kr] = S.record_u ? un[0] : vn[0];
-                }
-            }
-            if (isfe >= 0) {
 #pragma unroll
-                for (int f = 0; f < NV; f++)
-                    static_cast<float *>(S.ckpt)[((size_t)isfe * S.nf + base_ck + NV + f) * ncell + k] = vn[f];
+            for (int q = 0; q < QM; q++) {
+#pragma unroll
+                for (int w = 0; w < NWA; w++) wa[w][3] = P[(FS + 2 * w) * fs + q + 1];
+                const bool xS = (xs_mask >> q) & 1;
+                // ds = 0; ds = (x part) where xS; ds += (z part) where zS  (gb_stencil.h order)
+                float ds[NV];
+                if (PSV) {
+                    // sxx (x), sxz (x and z), szz (z)
+                    const float *c0 = P + (FS + 2) * fs + q, *b0 = P + (FS + 1) * fs + q;
+                    const float ax_ = st_dminus(wa[0][2], wa[0][1], wa[0][3], wa[0][0], c9x, c24x);
+                    const float az_ = st_dminus(wa[NWA - 1][2], wa[NWA - 1][1], wa[NWA - 1][3], wa[NWA - 1][0], c9x, c24x);
+                    const float bx_ = st_dminus(wa[NWA - 1][2], c0[-rs], c0[rs], c0[-2 * rs], c9z, c24z);
+                    const float bz_ = st_dminus(b0[0], b0[-rs], b0[rs], b0[-2 * rs], c9z, c24z);
+                    const float dsx = xS ? ax_ : 0.f, dsz = xS ? az_ : 0.f;
+                    ds[0] = zs ? dsx + bx_ : dsx;
+                    ds[NV - 1] = zs ? dsz + bz_ : dsz;
+                } else {
+                    const float *b0 = P + (FS + 1) * fs + q;
+                    const float ax_ = st_dminus(wa[0][2], wa[0][1], wa[0][3], wa[0][0], c9x, c24x);
+                    const float bz_ = st_dminus(b0[0], b0[-rs], b0[rs], b0[-2 * rs], c9z, c24z);
+                    const float dsy = xS ? ax_ : 0.f;
+                    ds[0] = zs ? dsy + bz_ : dsy;
+                }
+                int e = -1;  // receiver entry of this cell
+                if ((spm >> q) & 1) {
+                    if ((rmask >> q) & 1) e = rbase + __popc(rmask & ((1u << q) - 1u));
+                    if (!ADJ && q == srcq) {
+#pragma unroll
+                        for (int f = 0; f < NV; f++) ds[f] += sbuf[f];
+                    }
+                    if (ADJ && e >= 0) {
+#pragma unroll
+                        for (int f = 0; f < NV; f++) ds[f] += rbuf[e * NV + f];
+                    }
+                }
+                const float ab = s_ax[cb + q + 2] * azj;
+                float vn[NV], un[NV];
+#pragma unroll
+                for (int f = 0; f < NV; f++) {
+                    float *pv = P + (FV + f) * fs + q, *pu = P + (FU + f) * fs + q;
+                    vn[f] = st_velocity(ab, dt, ds[f], p_ri[q], *pv);
+                    un[f] = st_displacement(*pu, vn[f], dt);
+                    *pv = vn[f];
+                    *pu = un[f];
+                }
+                // ghosts: the left neighbour reads columns 0, 1, the right one column cp-1
+                if (q < 2 && eL) {
+                    const uint32_t a = lf + 4u * (uint32_t)(cp + q + 2);
+#pragma unroll
+                    for (int f = 0; f < NV; f++) {
+                        cl_st(a + 4u * (uint32_t)((FV + f) * fs), vn[f]);
+                        if (ADJ) cl_st(a + 4u * (uint32_t)((FU + f) * fs), un[f]);
+                    }
+                }
+                if (q == QM - 1 && eR) {
+                    const uint32_t a = rt + 4u;
+#pragma unroll
+                    for (int f = 0; f < NV; f++) {
+                        cl_st(a + 4u * (uint32_t)((FV + f) * fs), vn[f]);
+                        if (ADJ) cl_st(a + 4u * (uint32_t)((FU + f) * fs), un[f]);
+                    }
+                }
+                if (!ADJ && e >= 0) {
+#pragma unroll
+                    for (int f = 0; f < NV; f++) rbuf[e * NV + f] = S.record_u ? un[f] : vn[f];
+                }
+#pragma unroll
+                for (int w = 0; w < NWA; w++) {
+                    wa[w][0] = wa[w][1];
+                    wa[w][1] = wa[w][2];
+                    wa[w][2] = wa[w][3];
+                }
             }
         }
         cl.sync();
+        // Global traffic of the step, issued here so that phase B's work hides
+        // its latency before the next barrier: recorded samples, checkpoints
+        // of velocity (after this step's update) and displacement (before the
+        // next step; phase B changes neither), the next step's injection.
+        if (!ADJ) {
+#pragma unroll 1
+            for (int n = 0; n < nrq; n++) {
+                const int e = rbase + n;
+                const size_t kr = (size_t)rtab[e] * nt + it;
+                if (PSV) {
+                    S.out_x[kr] = rbuf[e * NV];
+                    S.out_z[kr] = rbuf[e * NV + NV - 1];
+                } else {
+                    S.out_y[kr] = rbuf[e * NV];
+                }
+            }
+            const int isfe = ckpt_of(it);
+            if (isfe >= 0) store_ckpt(isfe, FV, NV);
+            const int isfe_n = it + 1 < nt ? ckpt_of(it + 1) : -1;
+            if (isfe_n >= 0) store_ckpt(isfe_n, FU, 0);
+        }
+        prefetch(it + 1);
         // ---- phase B: velocity gradients and stress update
-        for (int q = 0; q < ncol; q++) {
-            const int i = x0 + grp + q * g.G;
-            const size_t k = (size_t)i * nz + row;
-            const bool xV = i >= 1 && i < nx - 2;
-            const bool inner = i - 1 >= x0 && i + 2 < x1;
-            float dxv[NV], dzv[NV];
+        {
+            float wb[NV][4];  // x-window: columns c-1, c, c+1, c+2
 #pragma unroll
             for (int f = 0; f < NV; f++) {
-                const float *v0 = own(FV + f, i);
-                dxv[f] = 0.f;
-                if (xV) {
-                    const float *vp1 = inner ? v0 + nz : col(FV + f, i + 1), *vp2 = inner ? v0 + 2 * nz : col(FV + f, i + 2),
-                                *vm1 = inner ? v0 - nz : col(FV + f, i - 1);
-                    dxv[f] = cdp(vp1[row], v0[row], vp2[row], vm1[row], c9x, c24x);
-                }
-                dzv[f] = zV ? cdp(v0[row + 1], v0[row], v0[row + 2], v0[row - 1], c9z, c24z) : 0.f;
+                const float *p = P + (FV + f) * fs;
+                wb[f][0] = p[-1];
+                wb[f][1] = p[0];
+                wb[f][2] = p[1];
             }
-            const float m = __ldg(S.mu + k);
-            if (PSV) {
-                const float l = __ldg(S.lambda + k);
-                float *sxx = own(FS + 0, i), *szz = own(FS + 1, i), *sxz = own(FS + 2, i);
-                float a = sxx[row], b = szz[row], c = sxz[row];
-                st_stress_psv(a, b, c, l, m, dt, dxv[0], dzv[0], dxv[1], dzv[1]);
-                sxx[row] = a;
-                szz[row] = b;
-                sxz[row] = c;
-            } else {
-                float *sxy = own(FS + 0, i), *szy = own(FS + 1, i);
-                float a = sxy[row], b = szy[row];
-                st_stress_sh(a, b, m, dt, dxv[0], dzv[0]);
-                sxy[row] = a;
-                szy[row] = b;
+#pragma unroll
+            for (int q = 0; q < QM; q++) {
+                const bool xV = (xv_mask >> q) & 1;
+                float dxv[NV], dzv[NV];
+#pragma unroll
+                for (int f = 0; f < NV; f++) {
+                    const float *v0 = P + (FV + f) * fs + q;
+                    wb[f][3] = v0[2];
+                    const float gx = st_dplus(wb[f][2], wb[f][1], wb[f][3], wb[f][0], c9x, c24x);
+                    const float gz = st_dplus(v0[rs], wb[f][1], v0[2 * rs], v0[-rs], c9z, c24z);
+                    dxv[f] = xV ? gx : 0.f;
+                    dzv[f] = zv ? gz : 0.f;
+                }
+                float *ps = P + FS * fs + q;
+                float sv[NSF];
+#pragma unroll
+                for (int f = 0; f < NSF; f++) sv[f] = ps[f * fs];
+                if (PSV)
+                    st_stress_psv(sv[0], sv[1], sv[NSF - 1], p_la[q], p_mu[q], dt, dxv[0], dzv[0], dxv[NV - 1],
+                                  dzv[NV - 1]);
+                else
+                    st_stress_sh(sv[0], sv[1], p_mu[q], dt, dxv[0], dzv[0]);
+#pragma unroll
+                for (int f = 0; f < NSF; f++) ps[f * fs] = sv[f];
+                // ghosts: the left neighbour reads column 0, the right one columns cp-2, cp-1
+                if (q == 0 && eL) {
+                    const uint32_t a = lf + 4u * (uint32_t)(cp + 2);
+#pragma unroll
+                    for (int f = 0; f < NSF; f++) cl_st(a + 4u * (uint32_t)((FS + f) * fs), sv[f]);
+                }
+                if (q >= QM - 2 && eR) {
+                    const uint32_t a = rt + 4u * (uint32_t)(q - QM + 2);
+#pragma unroll
+                    for (int f = 0; f < NSF; f++) cl_st(a + 4u * (uint32_t)((FS + f) * fs), sv[f]);
+                }
+#pragma unroll
+                for (int f = 0; f < NV; f++) {
+                    wb[f][0] = wb[f][1];
+                    wb[f][1] = wb[f][2];
+                    wb[f][2] = wb[f][3];
+                }
             }
         }
         cl.sync();
@@ -228,53 +393,47 @@ __global__ void __launch_bounds__(1024, 1) k_cluster(const Slot *__restrict__ sl
         if (ADJ && S.ckpt && S.sfe > 0 && it % S.sfe == 0 && it / S.sfe < S.nsfe) {
             const int isfe_a = it / S.sfe;
             const float ndt = (float)S.sfe * dt;
-            const int nfu = NV;
             float inv[4];
-            for (int q = 0; q < 2 * nfu; q++) {
+            for (int q = 0; q < 2 * NV; q++) {
                 const float a = S.ckpt_amax ? S.ckpt_amax[(size_t)isfe_a * S.nf + base_ck + q] : 0.f;
                 inv[q] = 1.f / ckpt_scale_of(a, S.ckpt_prec);
             }
             float *kl = kpart + ((size_t)slot * 3 + 0) * ncell;
             float *km = kpart + ((size_t)slot * 3 + 1) * ncell;
             float *kr = kpart + ((size_t)slot * 3 + 2) * ncell;
-            for (int q = 0; q < ncol; q++) {
-                const int i = x0 + grp + q * g.G;
-                const size_t k = (size_t)i * nz + row;
-                const bool gx = i >= 1 && i < nx - 2;
-                const bool inner = i - 1 >= x0 && i + 2 < x1;
+#pragma unroll 1
+            for (int q = 0; q < nq; q++) {
+                const size_t k = (size_t)(i0 + q) * nz + j;
+                const bool gx = (xv_mask >> q) & 1;
                 float ux[NV], uzz[NV], fx[NV], fz[NV];
 #pragma unroll
                 for (int f = 0; f < NV; f++) {
-                    const float *u0 = own(FU + f, i);
-                    ux[f] = 0.f;
-                    if (gx) {
-                        const float *up1 = inner ? u0 + nz : col(FU + f, i + 1), *up2 = inner ? u0 + 2 * nz : col(FU + f, i + 2),
-                                    *um1 = inner ? u0 - nz : col(FU + f, i - 1);
-                        ux[f] = cdp(up1[row], u0[row], up2[row], um1[row], c9x, c24x);
-                    }
-                    uzz[f] = zV ? cdp(u0[row + 1], u0[row], u0[row + 2], u0[row - 1], c9z, c24z) : 0.f;
+                    const float *u0 = P + (FU + f) * fs + q;
+                    ux[f] = gx ? st_dplus(u0[1], u0[0], u0[2], u0[-1], c9x, c24x) : 0.f;
+                    uzz[f] = zv ? st_dplus(u0[rs], u0[0], u0[2 * rs], u0[-rs], c9z, c24z) : 0.f;
                     const int qc = base_ck + f;
                     const float iv = inv[f];
-                    fx[f] = gx ? cdp(ck_get(S, isfe_a, qc, k + nz, ncell, iv), ck_get(S, isfe_a, qc, k, ncell, iv),
-                                     ck_get(S, isfe_a, qc, k + 2 * nz, ncell, iv),
-                                     ck_get(S, isfe_a, qc, k - nz, ncell, iv), c9x, c24x)
+                    fx[f] = gx ? st_dplus(ck_get(S, isfe_a, qc, k + nz, ncell, iv), ck_get(S, isfe_a, qc, k, ncell, iv),
+                                          ck_get(S, isfe_a, qc, k + 2 * nz, ncell, iv),
+                                          ck_get(S, isfe_a, qc, k - nz, ncell, iv), c9x, c24x)
                                : 0.f;
-                    fz[f] = zV ? cdp(ck_get(S, isfe_a, qc, k + 1, ncell, iv), ck_get(S, isfe_a, qc, k, ncell, iv),
-                                     ck_get(S, isfe_a, qc, k + 2, ncell, iv), ck_get(S, isfe_a, qc, k - 1, ncell, iv),
-                                     c9z, c24z)
+                    fz[f] = zv ? st_dplus(ck_get(S, isfe_a, qc, k + 1, ncell, iv), ck_get(S, isfe_a, qc, k, ncell, iv),
+                                          ck_get(S, isfe_a, qc, k + 2, ncell, iv),
+                                          ck_get(S, isfe_a, qc, k - 1, ncell, iv), c9z, c24z)
                                : 0.f;
                 }
+                const float *v0 = P + FV * fs + q;
                 if (PSV) {
-                    const float dvxdx = ux[0], dvxdz = uzz[0], dvzdx = ux[1], dvzdz = uzz[1];
-                    const float fxdx = fx[0], fxdz = fz[0], fzdx = fx[1], fzdz = fz[1];
+                    const float dvxdx = ux[0], dvxdz = uzz[0], dvzdx = ux[NV - 1], dvzdz = uzz[NV - 1];
+                    const float fxdx = fx[0], fxdz = fz[0], fzdx = fx[NV - 1], fzdz = fz[NV - 1];
                     const float vx_fw = ck_get(S, isfe_a, base_ck + 2, k, ncell, inv[2]);
                     const float vz_fw = ck_get(S, isfe_a, base_ck + 3, k, ncell, inv[3]);
-                    kr[k] -= (vx_fw * own(FV + 0, i)[row] + vz_fw * own(FV + 1, i)[row]) * ndt;
+                    kr[k] -= (vx_fw * v0[0] + vz_fw * v0[fs]) * ndt;
                     km[k] -= (2.f * dvxdx * fxdx + 2.f * dvzdz * fzdz + (dvxdz + dvzdx) * (fzdx + fxdz)) * ndt;
                     kl[k] -= ((dvxdx + dvzdz) * (fxdx + fzdz)) * ndt;
                 } else {
                     const float vy_fw = ck_get(S, isfe_a, 1, k, ncell, inv[1]);
-                    kr[k] -= vy_fw * own(FV, i)[row] * ndt;
+                    kr[k] -= vy_fw * v0[0] * ndt;
                     km[k] -= (ux[0] * fx[0] + uzz[0] * fz[0]) * ndt;
                 }
             }
@@ -301,42 +460,63 @@ __global__ void k_cluster_reduce(const float *__restrict__ kpart, int nslots, si
 }
 
 size_t cluster_smem_bytes(bool psv, const ClusterGeom &g, int nz) {
-    return (size_t)((psv ? 7 : 4) + 1) * g.cols_per * nz * 4;
+    const int nv = psv ? 2 : 1;
+    return ((size_t)(psv ? 7 : 4) * cluster_row_stride(g.cols_per) * (nz + 4) + (g.cols_per + 4) + g.nrec_cta +
+            (size_t)(g.nrec_cta + 1) * nv) *
+           4;
 }
 
 template <bool PSV, bool ADJ>
-static cudaError_t launch_cluster_t(const Slot *d_slots, int nslots, ClusterGeom g, int nz, float *kpart,
-                                    cudaStream_t st) {
-    const size_t smem = cluster_smem_bytes(PSV, g, nz);
-    cudaError_t e = cudaFuncSetAttribute(k_cluster<PSV, ADJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    if (g.R > 8) {
-        e = cudaFuncSetAttribute(k_cluster<PSV, ADJ>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-        if (e != cudaSuccess) return e;
+static void *cluster_kernel_q(int qm) {
+    switch (qm) {
+    case 4: return (void *)k_cluster<PSV, ADJ, 4>;
+    case 8: return (void *)k_cluster<PSV, ADJ, 8>;
+    case 12: return (void *)k_cluster<PSV, ADJ, 12>;
+    case 16: return (void *)k_cluster<PSV, ADJ, 16>;
+    case 24: return (void *)k_cluster<PSV, ADJ, 24>;
+    default: return nullptr;
     }
+}
+
+static void *cluster_kernel(bool psv, bool adj, int qm) {
+    if (psv) return adj ? cluster_kernel_q<true, true>(qm) : cluster_kernel_q<true, false>(qm);
+    return adj ? cluster_kernel_q<false, true>(qm) : cluster_kernel_q<false, false>(qm);
+}
+
+static cudaError_t cluster_attrs(const void *kern, size_t smem, int R) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess && R > 8) e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    return e;
+}
+
+static cudaLaunchConfig_t cluster_config(ClusterGeom g, int nz, int nslots, size_t smem, cudaStream_t st,
+                                         cudaLaunchAttribute *attr) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(g.R * nslots);
-    cfg.blockDim = dim3(g.rows_pad * g.G);
+    cfg.blockDim = dim3(g.G * nz);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
-    cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = g.R;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_cluster<PSV, ADJ>, d_slots, g, kpart);
+    return cfg;
 }
 
 cudaError_t launch_cluster(bool psv, bool adj, const Slot *d_slots, int nslots, ClusterGeom g, int nz, float *kpart,
                            cudaStream_t st) {
     if (nslots <= 0) return cudaSuccess;
-    if (psv)
-        return adj ? launch_cluster_t<true, true>(d_slots, nslots, g, nz, kpart, st)
-                   : launch_cluster_t<true, false>(d_slots, nslots, g, nz, kpart, st);
-    return adj ? launch_cluster_t<false, true>(d_slots, nslots, g, nz, kpart, st)
-               : launch_cluster_t<false, false>(d_slots, nslots, g, nz, kpart, st);
+    void *kern = cluster_kernel(psv, adj, g.qmax);
+    if (!kern) return cudaErrorInvalidValue;
+    const size_t smem = cluster_smem_bytes(psv, g, nz);
+    cudaError_t e = cluster_attrs(kern, smem, g.R);
+    if (e != cudaSuccess) return e;
+    cudaLaunchAttribute attr[1];
+    cudaLaunchConfig_t cfg = cluster_config(g, nz, nslots, smem, st, attr);
+    void *args[] = {(void *)&d_slots, (void *)&g, (void *)&kpart};
+    return cudaLaunchKernelExC(&cfg, kern, args);
 }
 
 cudaError_t launch_cluster_reduce(const float *kpart, int nslots, size_t ncell, float *kl, float *km, float *kr,
@@ -346,36 +526,27 @@ cudaError_t launch_cluster_reduce(const float *kpart, int nslots, size_t ncell, 
     return cudaGetLastError();
 }
 
-// Largest number of clusters of this geometry that can be resident at once
-// (0 when the geometry cannot launch).
+// Largest number of clusters of this geometry that can be resident at once,
+// for both passes (0 when the geometry cannot launch).
 int cluster_occupancy(bool psv, ClusterGeom g, int nz) {
     const size_t smem = cluster_smem_bytes(psv, g, nz);
-    auto kern = psv ? (void *)k_cluster<true, false> : (void *)k_cluster<false, false>;
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
-        (void)cudaGetLastError();
-        return 0;
+    int best = -1;
+    for (int adj = 0; adj < 2; adj++) {
+        void *kern = cluster_kernel(psv, adj != 0, g.qmax);
+        if (!kern || cluster_attrs(kern, smem, g.R) != cudaSuccess) {
+            (void)cudaGetLastError();
+            return 0;
+        }
+        cudaLaunchAttribute attr[1];
+        cudaLaunchConfig_t cfg = cluster_config(g, nz, 4, smem, nullptr, attr);
+        int n = 0;
+        if (cudaOccupancyMaxActiveClusters(&n, kern, &cfg) != cudaSuccess) {
+            (void)cudaGetLastError();
+            return 0;
+        }
+        best = best < 0 ? n : std::min(best, n);
     }
-    if (g.R > 8 && cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
-        (void)cudaGetLastError();
-        return 0;
-    }
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(g.R * 4);
-    cfg.blockDim = dim3(g.rows_pad * g.G);
-    cfg.dynamicSmemBytes = smem;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = g.R;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    int n = 0;
-    if (cudaOccupancyMaxActiveClusters(&n, kern, &cfg) != cudaSuccess) {
-        (void)cudaGetLastError();
-        return 0;
-    }
-    return n;
+    return std::max(best, 0);
 }
 
 }  // namespace gb

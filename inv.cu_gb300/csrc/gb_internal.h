@@ -77,10 +77,17 @@ struct TileCfg {
 };
 
 // Cluster-resident solver geometry: R CTAs per shot (cluster), cols_per grid
-// columns per CTA, rows_pad = nz rounded up to 32, G column groups per CTA
-// (blockDim = rows_pad * G).
+// columns per CTA (a multiple of qmax; the last CTA holds the remaining grid
+// columns, at least 2), G groups of nz threads per CTA (blockDim = G * nz),
+// each thread owning qmax consecutive columns of one row (qmax in
+// {4, 8, 12, 16, 24}, G * qmax = cols_per); nrec_cta = most receivers in one
+// CTA's columns.
+// The launch also carries the values common to all slots (grid, steps, time
+// step and stencil coefficients), which the kernel reads from its parameters.
 struct ClusterGeom {
-    int R, cols_per, G, rows_pad;
+    int R, cols_per, G, qmax, nrec_cta;
+    int nx, nz, nt;
+    float dt, c9x, c24x, c9z, c24z;
 };
 
 // Power-of-two scale of a 16-bit checkpoint with max |value| amax: FP16 maps
@@ -121,6 +128,7 @@ cudaError_t launch_fill(float *p, float v, size_t n, cudaStream_t st);
 // Cluster-resident passes (gb_cluster.cu): one cluster per slot runs the
 // whole pass; the adjoint adds each slot's kernels to kpart[slot][3][nx*nz].
 size_t cluster_smem_bytes(bool psv, const ClusterGeom &g, int nz);
+int cluster_max_threads(bool psv, int qmax);
 int cluster_occupancy(bool psv, ClusterGeom g, int nz);
 cudaError_t launch_cluster(bool psv, bool adj, const Slot *d_slots, int nslots, ClusterGeom g, int nz, float *kpart,
                            cudaStream_t st);

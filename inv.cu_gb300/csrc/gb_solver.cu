@@ -11,6 +11,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <iostream>
 #include <map>
@@ -168,7 +170,7 @@ int Solver::init(const Config &cfg, int nx_, int nz_, float xmax_, float zmax_) 
     if (cfg.has("graphs")) opt_graphs = cfg.iv("graphs") != 0;
     if (cfg.has("ckpt_precision")) opt_ckpt = cfg.iv("ckpt_precision");
     if (cfg.has("tile")) opt_tile = cfg.iv("tile");
-    if (cfg.has("cluster")) opt_cluster = cfg.iv("cluster") != 0;
+    if (cfg.has("cluster")) opt_cluster = std::max(0, std::min(16, cfg.iv("cluster")));
     nx = nx_;
     nz = nz_;
     xmax = xmax_;
@@ -738,34 +740,48 @@ int Solver::run_pass(int kind, int n, bool snapshot, int snap_isrc) {
 }
 
 // Cluster geometry for one wave system: R CTAs per shot, each holding
-// cols_per columns of the state (plus a receiver map) in shared memory.
-// Chooses the R with the fewest (cluster rounds x columns per thread).
+// cols_per columns of the state (plus ghost columns) in shared memory. The
+// cost model is the per-SM work of one step (cells per CTA plus a barrier
+// allowance) times the number of cluster rounds the batch needs.
 bool Solver::cluster_geometry(bool wave_psv, int n, ClusterGeom *out) const {
-    if (nz > 1024 || nx < 2) return false;
-    const int rows_pad = (nz + 31) / 32 * 32;
-    const int gmax = 1024 / rows_pad;
-    const size_t limit = 227 * 1024;
-    long best = -1;
-    for (int R = 2; R <= 16; R++) {
-        ClusterGeom g;
-        g.R = R;
-        g.cols_per = (nx + R - 1) / R;
-        g.rows_pad = rows_pad;
-        g.G = std::min(gmax, g.cols_per);
-        if (g.cols_per < 3 || cluster_smem_bytes(wave_psv, g, nz) > limit) continue;
-        const int occ = cluster_occupancy(wave_psv, g, nz);
-        if (occ < 1) continue;
-        const long cost = (long)((n + occ - 1) / occ) * ((g.cols_per + g.G - 1) / g.G);
-        if (best < 0 || cost < best) {
-            best = cost;
-            *out = g;
+    if (nx < 2 || nz < 1) return false;
+    static const bool trace = std::getenv("GBFWI_TRACE") != nullptr;  // print the candidates to stderr
+    const size_t limit = 227 * 1024 - 64;  // dynamic shared memory, beside the kernel's static counter
+    double best = -1;
+    const int rlo = opt_cluster >= 2 ? opt_cluster : 1, rhi = opt_cluster >= 2 ? opt_cluster : 16;
+    for (int R = rlo; R <= rhi; R++) {
+        for (int qm : {4, 8, 12, 16, 24}) {
+            ClusterGeom g;
+            g.R = R;
+            g.qmax = qm;
+            g.cols_per = ((nx + R - 1) / R + qm - 1) / qm * qm;
+            g.G = g.cols_per / qm;
+            if (nx - (R - 1) * g.cols_per < 2 || (long)g.G * nz > cluster_max_threads(wave_psv, qm)) continue;
+            std::vector<int> per(R, 0);
+            for (int r = 0; r < nrec; r++)
+                if (rec_xi[r] >= 0 && rec_xi[r] < nx && rec_zi[r] >= 0 && rec_zi[r] < nz)
+                    per[rec_xi[r] / g.cols_per]++;
+            g.nrec_cta = *std::max_element(per.begin(), per.end());
+            if (cluster_smem_bytes(wave_psv, g, nz) > limit) continue;
+            const int occ = cluster_occupancy(wave_psv, g, nz);
+            if (trace)
+                std::fprintf(stderr, "gbfwi cluster %s R=%d cols=%d qmax=%d threads=%d smem=%zu clusters=%d\n",
+                             wave_psv ? "psv" : "sh", R, g.cols_per, g.qmax, g.G * nz,
+                             cluster_smem_bytes(wave_psv, g, nz), occ);
+            if (occ < 1) continue;
+            const double cost = (double)((n + occ - 1) / occ) * ((double)g.cols_per * nz + 6000.0);
+            if (best < 0 || cost < best) {
+                best = cost;
+                *out = g;
+            }
         }
     }
     return best >= 0;
 }
 
 bool Solver::cluster_ok(const int *shots, int n, bool snapshot) const {
-    if (!opt_cluster || snapshot || !rec_distinct || opt_ckpt != CKPT_F32) return false;
+    // receiver ids are held as 16-bit values inside the kernel
+    if (!opt_cluster || snapshot || !rec_distinct || opt_ckpt != CKPT_F32 || nrec >= 0xffff) return false;
     for (int b = 0; b < n; b++)
         if (shots[b] < 0) return false;
     ClusterGeom g;
@@ -797,6 +813,15 @@ int Solver::run_cluster_pass(int kind, int n) {
             set_error("cluster pass: no geometry fits");
             return GB_ERR_STATE;
         }
+        // the same values as every slot's (fill_slots)
+        g.nx = nx;
+        g.nz = nz;
+        g.nt = nt;
+        g.dt = dt;
+        g.c9x = 9.f / (8.f * dx);
+        g.c24x = 1.f / (24.f * dx);
+        g.c9z = 9.f / (8.f * dz);
+        g.c24z = 1.f / (24.f * dz);
         GB_CUDA_TRY(launch_cluster(wp, adjp, d_slots[kind], n, g, nz, adjp ? kpart : nullptr, st));
         stats.launches += 1;
         if (adjp) {

@@ -59,7 +59,7 @@ struct Solver {
     int opt_ckpt = CKPT_F32;
     int opt_tile = 0;  // 0 = autotune
     double opt_budget_gb = 0;
-    bool opt_cluster = true;  // cluster-resident passes when the state fits on chip
+    int opt_cluster = 1;  // cluster-resident passes: 0 never, 1 automatic R, 2..16 this cluster size
 
     // device buffers in the reference layout
     float *lambda = nullptr, *mu = nullptr, *rho = nullptr;

@@ -51,6 +51,32 @@ def test_cluster_pass_matches_step_kernels(gpu, orc, wave, nx, nz, nt):
         assert cases.rel(k_c[n], k_t[n]) < 1e-6, n
 
 
+@pytest.mark.parametrize("wave,nx,size", [("psv", 94, 1), ("psv", 94, 2), ("psv", 94, 3), ("psv", 94, 5),
+                                          ("psv", 94, 8), ("psv", 94, 12), ("psv", 50, 4), ("sh", 94, 1),
+                                          ("sh", 94, 4), ("sh", 94, 12), ("sh", 50, 4)])
+def test_cluster_sizes_match_step_kernels(gpu, orc, wave, nx, size):
+    """Cluster sizes (1 = automatic); 94 columns at 12 CTAs leave the last CTA
+    6 columns, 50 at 4 CTAs (16 columns each) leave it 2. Receivers are
+    scattered over the grid: several per thread, per CTA and at CTA edges."""
+    nz, nt = 40, 150
+    case = cases.make_case(wave=wave, nx=nx, nz=nz, nt=nt, nsrc=2, nrec=60, sfe=10, seed=size)
+    rng = np.random.default_rng(size)
+    cells = rng.choice(nx * nz, 60, replace=False)
+    case["rec"] = [[float(c // nz) * 10.0, float(c % nz) * 10.0] for c in cells]
+    ad = [{c: (rng.standard_normal((60, nt)) * 1e-3).astype(np.float32) for c in "xyz"} for _ in range(2)]
+    tr_c, k_c, st_c = run(gpu, case, size, ad)
+    tr_t, k_t, st_t = run(gpu, case, 0, ad)
+    if size == 1:  # automatic size
+        assert st_c.tile_tz < 0, "the cluster path did not run"
+    else:
+        assert st_c.tile_tz == -size, "the cluster path did not run with this size"
+    for b in range(2):
+        for c in comps(wave):
+            np.testing.assert_array_equal(tr_c[b][c], tr_t[b][c])
+    for n in names(wave):
+        assert cases.rel(k_c[n], k_t[n]) < 1e-6, n
+
+
 def test_cluster_adjoint_matches_oracle(gpu, orc):
     case = cases.make_case(wave="psv", nx=120, nz=96, nt=400, nsrc=2, nrec=40, sfe=10, seed=11)
     pb = cases.oracle_problem(orc, case)
