@@ -370,6 +370,8 @@ def run_ours(args, ws, rank, local):
                        ckpt="fp32", parallelism="shots sharded over %d rank(s), replicas" % ws),
         "cell_updates_per_s": round(2.0 * cells * NT * NSHOT * args.steps * ws / (total_ms / 1e3), 1),
         "misfit": mis_val, "plain_path": plain, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+        "breakdown_ms_per_gradient": {k: round(getattr(st, k) / args.steps, 3)
+                                      for k in ("forward_ms", "adjoint_ms", "misfit_ms", "filter_ms")},
         "gpu_launches": int(st.launches), "clocks": clocks,
     }
     if rank == 0:
@@ -598,6 +600,27 @@ def run_profile_case(args):
 
     pkg = ge.load_package()
     name = args.profile_case
+    if name == "sh-c2-nt200":
+        # the headline workload's shapes (16 shots, 681 receivers, checkpoints
+        # every 10 steps) over 200 steps: one forward and one adjoint pass
+        wl = workload()
+        cfg = pkg.Config.new(tempfile.mkdtemp(prefix="gbfwi_prof_"), dict(wl["values"], nt=200), wl["src"], wl["rec"])
+        sol = pkg.FdmSolver(cfg, grid=(NX, NZ, wl["xmax"], wl["zmax"]))
+        sol.set_option("batch", NSHOT)
+        sol.set_option("graphs", 0)
+        sol.set_option("cluster", args.cluster)
+        sol.set_model_grid(*wl["init"])
+        shots = list(range(NSHOT))
+        sol.run_forward_batch(shots)
+        rng = np.random.default_rng(0)
+        for b in shots:
+            sol.set_adstf("y", (rng.standard_normal((NX, 200)) * 1e-3).astype(np.float32), slot=b)
+        sol.initKernels()
+        sol.run_adjoint_batch(shots)
+        st = sol.stats()
+        print("profile case", name, "cluster", args.cluster, "forward_ms %.3f adjoint_ms %.3f" % (st.forward_ms,
+                                                                                            st.adjoint_ms))
+        return
     if name == "psv-2048x1024x2":
         case = cases.make_case(wave="psv", nx=2048, nz=1024, nt=12, nsrc=2, nrec=256, seed=1, abs_width=20)
     elif name == "sh-681x141x16":

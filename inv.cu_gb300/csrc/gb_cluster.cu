@@ -390,51 +390,62 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
         }
         cl.sync();
         // ---- adjoint: kernel accumulation every sfe steps (solver/fdm.h:583-606)
+        // FP32 checkpoints (the only precision this path takes): the
+        // x-differences walk the thread's columns with a window over the
+        // checkpointed displacement, so each column adds one checkpoint load
+        // per field; rows and columns are clamped to the grid, and a cell's
+        // differences are masked where the reference skips them.
         if (ADJ && S.ckpt && S.sfe > 0 && it % S.sfe == 0 && it / S.sfe < S.nsfe) {
             const int isfe_a = it / S.sfe;
             const float ndt = (float)S.sfe * dt;
-            float inv[4];
-            for (int q = 0; q < 2 * NV; q++) {
-                const float a = S.ckpt_amax ? S.ckpt_amax[(size_t)isfe_a * S.nf + base_ck + q] : 0.f;
-                inv[q] = 1.f / ckpt_scale_of(a, S.ckpt_prec);
-            }
-            float *kl = kpart + ((size_t)slot * 3 + 0) * ncell;
-            float *km = kpart + ((size_t)slot * 3 + 1) * ncell;
-            float *kr = kpart + ((size_t)slot * 3 + 2) * ncell;
-#pragma unroll 1
-            for (int q = 0; q < nq; q++) {
-                const size_t k = (size_t)(i0 + q) * nz + j;
-                const bool gx = (xv_mask >> q) & 1;
-                float ux[NV], uzz[NV], fx[NV], fz[NV];
+            const float *ckb = static_cast<const float *>(S.ckpt) + ((size_t)isfe_a * S.nf + base_ck) * ncell;
+            const size_t kc = (size_t)i0 * nz + j;  // this thread's first cell
+            const int zm = zv ? -1 : 0, zp = zv ? 1 : 0, zp2 = zv ? 2 : 0;
+            auto colk = [&](int q) -> size_t { return (size_t)min(max(i0 + q, 0), nx - 1) * nz + j; };
+            float cw[NV][4];  // checkpointed displacement f at columns c-1, c, c+1, c+2
 #pragma unroll
-                for (int f = 0; f < NV; f++) {
-                    const float *u0 = P + (FU + f) * fs + q;
-                    ux[f] = gx ? st_dplus(u0[1], u0[0], u0[2], u0[-1], c9x, c24x) : 0.f;
-                    uzz[f] = zv ? st_dplus(u0[rs], u0[0], u0[2 * rs], u0[-rs], c9z, c24z) : 0.f;
-                    const int qc = base_ck + f;
-                    const float iv = inv[f];
-                    fx[f] = gx ? st_dplus(ck_get(S, isfe_a, qc, k + nz, ncell, iv), ck_get(S, isfe_a, qc, k, ncell, iv),
-                                          ck_get(S, isfe_a, qc, k + 2 * nz, ncell, iv),
-                                          ck_get(S, isfe_a, qc, k - nz, ncell, iv), c9x, c24x)
-                               : 0.f;
-                    fz[f] = zv ? st_dplus(ck_get(S, isfe_a, qc, k + 1, ncell, iv), ck_get(S, isfe_a, qc, k, ncell, iv),
-                                          ck_get(S, isfe_a, qc, k + 2, ncell, iv),
-                                          ck_get(S, isfe_a, qc, k - 1, ncell, iv), c9z, c24z)
-                               : 0.f;
-                }
-                const float *v0 = P + FV * fs + q;
-                if (PSV) {
-                    const float dvxdx = ux[0], dvxdz = uzz[0], dvzdx = ux[NV - 1], dvzdz = uzz[NV - 1];
-                    const float fxdx = fx[0], fxdz = fz[0], fzdx = fx[NV - 1], fzdz = fz[NV - 1];
-                    const float vx_fw = ck_get(S, isfe_a, base_ck + 2, k, ncell, inv[2]);
-                    const float vz_fw = ck_get(S, isfe_a, base_ck + 3, k, ncell, inv[3]);
-                    kr[k] -= (vx_fw * v0[0] + vz_fw * v0[fs]) * ndt;
-                    km[k] -= (2.f * dvxdx * fxdx + 2.f * dvzdz * fzdz + (dvxdz + dvzdx) * (fzdx + fxdz)) * ndt;
-                    kl[k] -= ((dvxdx + dvzdz) * (fxdx + fzdz)) * ndt;
-                } else {
-                    const float vy_fw = ck_get(S, isfe_a, 1, k, ncell, inv[1]);
-                    kr[k] -= vy_fw * v0[0] * ndt;
-                    km[k] -= (ux[0] * fx[0] + uzz[0] * fz[0]) * ndt;
+            for (int f = 0; f < NV; f++) {
+                const float *u = ckb + (size_t)f * ncell;
+                cw[f][0] = __ldg(u + colk(-1));
+                cw[f][1] = __ldg(u + colk(0));
+                cw[f][2] = __ldg(u + colk(1));
+            }
+            float *kl = kpart + ((size_t)slot * 3 + 0) * ncell + kc;
+            float *km = kpart + ((size_t)slot * 3 + 1) * ncell + kc;
+            float *kr = kpart + ((size_t)slot * 3 + 2) * ncell + kc;
+#pragma unroll 1
+            for (int q = 0; q < QM; q++) {
+                if (q < nq) {
+                    const bool gx = (xv_mask >> q) & 1;
+                    float ux[NV], uzz[NV], fx[NV], fz[NV], vf[NV];
+#pragma unroll
+                    for (int f = 0; f < NV; f++) {
+                        const float *u = ckb + (size_t)f * ncell;
+                        cw[f][3] = __ldg(u + colk(q + 2));
+                        const float *uc = u + kc + (size_t)q * nz;
+                        vf[f] = __ldg(uc + (size_t)NV * ncell);  // checkpointed velocity f
+                        const float *u0 = P + (FU + f) * fs + q;
+                        ux[f] = gx ? st_dplus(u0[1], u0[0], u0[2], u0[-1], c9x, c24x) : 0.f;
+                        uzz[f] = zv ? st_dplus(u0[rs], u0[0], u0[2 * rs], u0[-rs], c9z, c24z) : 0.f;
+                        fx[f] = gx ? st_dplus(cw[f][2], cw[f][1], cw[f][3], cw[f][0], c9x, c24x) : 0.f;
+                        fz[f] = zv ? st_dplus(__ldg(uc + zp), cw[f][1], __ldg(uc + zp2), __ldg(uc + zm), c9z, c24z)
+                                   : 0.f;
+                        cw[f][0] = cw[f][1];
+                        cw[f][1] = cw[f][2];
+                        cw[f][2] = cw[f][3];
+                    }
+                    const float *v0 = P + FV * fs + q;
+                    const size_t o = (size_t)q * nz;
+                    if (PSV) {
+                        const float dvxdx = ux[0], dvxdz = uzz[0], dvzdx = ux[NV - 1], dvzdz = uzz[NV - 1];
+                        const float fxdx = fx[0], fxdz = fz[0], fzdx = fx[NV - 1], fzdz = fz[NV - 1];
+                        kr[o] -= (vf[0] * v0[0] + vf[NV - 1] * v0[fs]) * ndt;
+                        km[o] -= (2.f * dvxdx * fxdx + 2.f * dvzdz * fzdz + (dvxdz + dvzdx) * (fzdx + fxdz)) * ndt;
+                        kl[o] -= ((dvxdx + dvzdz) * (fxdx + fzdz)) * ndt;
+                    } else {
+                        kr[o] -= vf[0] * v0[0] * ndt;
+                        km[o] -= (ux[0] * fx[0] + uzz[0] * fz[0]) * ndt;
+                    }
                 }
             }
             cl.sync();
