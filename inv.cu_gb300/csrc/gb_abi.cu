@@ -300,7 +300,10 @@ int gb_solver_set_option(gb_solver *s, const char *key, double value) {
         const int t = (int)value;
         if (t < 0 || t > 20) return GB_ERR_ARG;
         v.opt_tile = t;
-        if (t == 0) v.tile_id = 0;
+        if (t == 0) {
+            v.tile_id = 0;
+            v.tuned = false;
+        }
         v.invalidate_graphs();
     } else if (k == "cluster") {
         const int c = (int)value;

@@ -745,6 +745,12 @@ int Solver::run_pass(int kind, int n, bool snapshot, int snap_isrc) {
 // allowance) times the number of cluster rounds the batch needs.
 bool Solver::cluster_geometry(bool wave_psv, int n, ClusterGeom *out) const {
     if (nx < 2 || nz < 1) return false;
+    const long long key = ((long long)n * 32 + opt_cluster) * 2 + (wave_psv ? 1 : 0);
+    const auto hit = cluster_cache.find(key);
+    if (hit != cluster_cache.end()) {
+        if (hit->second.first) *out = hit->second.second;
+        return hit->second.first;
+    }
     static const bool trace = std::getenv("GBFWI_TRACE") != nullptr;  // print the candidates to stderr
     const size_t limit = 227 * 1024 - 64;  // dynamic shared memory, beside the kernel's static counter
     double best = -1;
@@ -776,6 +782,7 @@ bool Solver::cluster_geometry(bool wave_psv, int n, ClusterGeom *out) const {
             }
         }
     }
+    cluster_cache[key] = {best >= 0, best >= 0 ? *out : ClusterGeom{}};
     return best >= 0;
 }
 
@@ -858,13 +865,15 @@ int Solver::forward(const int *shots, int n, bool ckpt_on, bool record_u, bool s
         }
     int rc = ensure_slots(n);
     if (rc) return rc;
-    if (opt_tile == 0 && tile_id == 0) {
+    // the tile configuration is tuned on the first pass that uses the per-step kernels
+    if (opt_tile == 0 && !tuned && !cluster_ok(shots, n, snapshot)) {
         rc = ensure_tables();
         if (rc) return rc;
         rc = fill_slots(PASS_FWD_NOCKPT, shots, n, record_u);
         if (rc) return rc;
         rc = autotune(n);
         if (rc) return rc;
+        tuned = true;
         cudaFree(d_csr);
         d_csr = nullptr;
         invalidate_graphs();

@@ -83,6 +83,7 @@ struct Solver {
 
     // tile tables
     int tile_id = 0;
+    bool tuned = false;  // the autotuner ran for the current options
     TileCfg tile{32, 32};
     int *d_csr = nullptr;
     size_t csr_words = 0;
@@ -120,6 +121,8 @@ struct Solver {
     int run_pass(int kind, int n, bool snapshot, int snap_isrc);
     int autotune(int n);
     bool cluster_geometry(bool wave_psv, int n, ClusterGeom *g) const;
+    // cluster_geometry results by (wave system, batch size, cluster option)
+    mutable std::map<long long, std::pair<bool, ClusterGeom>> cluster_cache;
     bool cluster_ok(const int *shots, int n, bool snapshot) const;
     int run_cluster_pass(int kind, int n);
     int export_snapshot(int it, int isrc, int par);
