@@ -71,7 +71,7 @@ struct KernelGroup {
 
 // Configuration of the fused step kernel. threads == 0: 2-D tile kernel
 // owning tz x tx cells per block. threads > 0: marching kernel, one grid row
-// per thread, tz = threads - 6 owned rows per strip, tx = columns per chunk.
+// per thread, tz = threads - 8 owned rows per strip, tx = columns per chunk.
 struct TileCfg {
     int tz, tx, threads;
 };

@@ -2,8 +2,9 @@
 //
 // A block of T threads owns a z-strip (one grid row per thread) and marches
 // along x over a chunk of C columns. Window rows are [w0, w0 + T) with
-// w0 = strip * (T - 6) - 3; rows [w0 + 3, w0 + T - 3) are owned, the three
-// rows above and below are the halo the stencil needs. At column step p the
+// w0 = strip * (T - 8) - 4, a multiple of 4 (16-byte aligned rows for bulk
+// copies); rows [w0 + 4, w0 + T - 4) are owned, the stencil reads three rows
+// of halo on either side (the window holds four). At column step p the
 // block
 //   * loads stress at column p (the x-neighbours of earlier columns stay in a
 //     4-deep register queue per thread),
@@ -80,7 +81,7 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
     constexpr int NS = W::NS, NV = W::NV;
     constexpr int NZS = PSV ? 2 : 1;  // stress components with a z-derivative (sxz, szz | szy)
     extern __shared__ float smem[];
-    const int T = blockDim.x, O = T - 6;
+    const int T = blockDim.x, O = T - 8;
     const int TP = T + 4;  // exchange rows padded by 2 on both sides
     float *ring = smem;                                  // [kRing][W::N][T]
     float *s_sz = ring + kRing * W::N * T;               // [2][NZS][TP]
@@ -96,11 +97,11 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
     if (tile >= S.tiles_z * S.tiles_x) return;
     const int strip = tile % S.tiles_z, ck = tile / S.tiles_z;
     const int t = threadIdx.x;
-    const int j = strip * O - 3 + t;          // grid row of this thread
+    const int j = strip * O - 4 + t;          // grid row of this thread
     const int c0 = ck * chunk;                 // first owned column
     const int c1 = min(c0 + chunk, nx);        // one past the last owned column
     const bool rowin = (unsigned)j < (unsigned)nz;
-    const bool rowown = t >= 3 && t < T - 3 && rowin;
+    const bool rowown = t >= 4 && t < T - 4 && rowin;
     const bool zS = j >= 2 && j < nz - 2;      // z part of the stress divergence
     const bool zV = j >= 1 && j < nz - 2;      // z part of the velocity gradient
     const float dt = S.dt, c9x = S.c9x, c24x = S.c24x, c9z = S.c9z, c24z = S.c24z;
@@ -213,6 +214,11 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
         if (q < nstep) issue(p_first + q, q);
         cpa_commit();
     }
+    // P-SV: unrolled by the queue depth, so the register queues rotate by
+    // renaming (fewer registers and moves); SH keeps the rolled loop, which
+    // fits its registers better
+    constexpr int kUnroll = PSV ? 4 : 1;
+#pragma unroll kUnroll
     for (int q = 0; q < nstep; q++) {
         const int p = p_first + q;
         cpa_wait<kRing - 2>();  // column step q has landed (own row)
@@ -266,7 +272,7 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
             // sources at this column, in trace order (solver/fdm.h:163-180)
             const int cl = pv - (c0 - 1);
             while (inj_next < (cl + 1) * VZ) {
-                if (t == inj_next - cl * VZ + 2) {
+                if (t == inj_next - cl * VZ + 3) {
                     for (int e = inj_tptr[inj_ptr]; e < inj_tptr[inj_ptr + 1]; e++) {
                         const int ks = inj_traces[e] * nt + it;
                         if (PSV) {
@@ -301,7 +307,7 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
                 }
                 // receivers (solver/fdm.h:181-196): u when record_u, else v
                 while (rec_next < (oc + 1) * O) {
-                    if (rowown && t == rec_next - oc * O + 3) {
+                    if (rowown && t == rec_next - oc * O + 4) {
                         for (int e = rec_tptr[rec_ptr]; e < rec_tptr[rec_ptr + 1]; e++) {
                             const int kr = rec_traces[e] * nt + it;
                             if (PSV) {

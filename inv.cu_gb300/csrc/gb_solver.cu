@@ -27,9 +27,9 @@ namespace gb {
 static const TileCfg kTiles[] = {
     {32, 32, 0},                                                            // 0: unused
     {32, 32, 0},   {64, 16, 0},   {32, 16, 0},   {16, 32, 0},   {128, 8, 0},  // 1-5
-    {58, 32, 64},  {90, 32, 96},  {122, 32, 128}, {122, 64, 128}, {154, 32, 160},  // 6-10
-    {154, 64, 160}, {186, 32, 192}, {250, 32, 256}, {250, 64, 256}, {122, 16, 128}, // 11-15
-    {58, 16, 64},  {250, 128, 256}, {122, 128, 128}, {154, 128, 160}, {154, 16, 160}, // 16-20
+    {56, 32, 64},  {88, 32, 96},  {120, 32, 128}, {120, 64, 128}, {152, 32, 160},  // 6-10
+    {152, 64, 160}, {184, 32, 192}, {248, 32, 256}, {248, 64, 256}, {120, 16, 128}, // 11-15
+    {56, 16, 64},  {248, 128, 256}, {120, 128, 128}, {152, 128, 160}, {152, 16, 160}, // 16-20
 };
 static const int kNumTiles = 20;
 
