@@ -137,14 +137,19 @@ int gb_solver_batch_capacity(gb_solver *s);
  * "ckpt" (0 FP32, 1 BF16, 2 FP16), "tile" (0 autotune, 1..20 fixed),
  * "cluster" (1: run whole passes in thread-block clusters when a shot's
  * state fits in their shared memory, with the cluster size chosen by
- * occupancy; 2..16: that cluster size; 0: never), "hbm_budget_gb". Options
+ * occupancy; 2..16: that cluster size; 0: never), "tma" (1: the marching
+ * kernel loads grid columns with bulk tensor copies when nz % 4 == 0,
+ * default; 0: per-thread cp.async), "hbm_budget_gb". Options
  * change no forward result; "ckpt" changes kernels by the checkpoint
  * rounding and "cluster" by the order in which shots are summed. */
 int gb_solver_set_option(gb_solver *s, const char *key, double value);
 
 /* Timing of the solver since the last reset (CUDA events on the solver's
  * stream). step_ms / step_launches: fused step kernels timed in windows of
- * consecutive launches; launches: kernels (or graph kernel nodes) enqueued. */
+ * consecutive launches; launches: kernels (or graph kernel nodes) enqueued.
+ * tile_tz, tile_tx: kernel configuration of the last pass (tile_tz = -R for
+ * a cluster-resident pass of R-CTA clusters); march_bulk: 1 when the last
+ * marching-kernel pass loaded its columns with bulk tensor copies. */
 typedef struct {
     double forward_ms, adjoint_ms, misfit_ms, filter_ms;
     double step_ms;
@@ -152,6 +157,7 @@ typedef struct {
     long long launches;
     long long cell_updates;
     int tile_tz, tile_tx, batch_capacity;
+    int march_bulk;
 } gb_stats;
 int gb_solver_stats(gb_solver *s, gb_stats *out, int reset);
 

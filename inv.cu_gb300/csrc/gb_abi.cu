@@ -305,6 +305,9 @@ int gb_solver_set_option(gb_solver *s, const char *key, double value) {
             v.tuned = false;
         }
         v.invalidate_graphs();
+    } else if (k == "tma") {
+        v.opt_tma = value != 0;
+        v.invalidate_graphs();
     } else if (k == "cluster") {
         const int c = (int)value;
         if (c < 0 || c > 16) return GB_ERR_ARG;
@@ -346,10 +349,12 @@ int gb_solver_stats(gb_solver *s, gb_stats *out, int reset) {
     if (out) *out = s->s.stats;
     if (reset) {
         const int tz = s->s.stats.tile_tz, tx = s->s.stats.tile_tx, cap = s->s.stats.batch_capacity;
+        const int bulk = s->s.stats.march_bulk;
         s->s.stats = gb_stats{};
         s->s.stats.tile_tz = tz;
         s->s.stats.tile_tx = tx;
         s->s.stats.batch_capacity = cap;
+        s->s.stats.march_bulk = bulk;
     }
     return GB_OK;
 }

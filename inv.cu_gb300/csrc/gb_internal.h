@@ -59,7 +59,16 @@ struct Slot {
     void *ckpt;
     float *ckpt_amax;
     int nsfe, nf, ckpt_prec;
+    // tensor maps (128-byte CUtensorMap each) of this slot's fields for the
+    // marching kernel's bulk loads, indexed by TMAP_*; null when unused
+    const void *tmap;
 };
+
+// Tensor map index of a P-SV field f (FieldPsv), an SH field (TMAP_SH + FieldSh)
+// and the model fields. Each map covers one field as a 2-D tensor {nz, nx}
+// with a box of {marching threads, TMAP_BOX_COLS} (rows, columns).
+constexpr int TMAP_SH = NPSV, TMAP_RINV = NPSV + NSH, TMAP_MU = TMAP_RINV + 1, TMAP_LAM = TMAP_RINV + 2,
+              TMAP_N = TMAP_RINV + 3, TMAP_BYTES = 128, TMAP_BOX_COLS = 4;
 
 // A group of slots that accumulate into the same sensitivity kernels.
 struct KernelGroup {
@@ -110,9 +119,13 @@ inline int csr_words(int ntiles, int nent, int ntr) { return 3 + ntiles + 1 + ne
 // ---------------------------------------------------------------- launchers
 // All launchers enqueue on `st` and return cudaGetLastError().
 // k is the launch's step index (see Slot::it_base).
-cudaError_t launch_step(bool psv, TileCfg tc, const Slot *d_slots, int nslots, int max_tiles, int k,
+cudaError_t launch_step(bool psv, TileCfg tc, const Slot *d_slots, int nslots, int max_tiles, int k, bool tma,
                         cudaStream_t st);
-cudaError_t launch_march(bool psv, int threads, int chunk, const Slot *d_slots, int nslots, int max_tiles, int k,
+// Marching kernel launch; tma = bulk tensor loads through the slots' maps.
+// march_tma_error returns (and clears) the device flag a bulk-load wait that
+// ran out of iterations sets.
+int march_tma_error();
+cudaError_t launch_march(bool psv, bool tma, int threads, int chunk, const Slot *d_slots, int nslots, int max_tiles, int k,
                          cudaStream_t st);
 // Checkpoint of displacement before step k (which_u = 1) or velocity after
 // it (which_u = 0), for every slot with ckpt_write whose step is a

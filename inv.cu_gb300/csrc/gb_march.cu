@@ -47,6 +47,10 @@ struct CsrM {
 
 constexpr int kMaxMarchThreads = 256;
 constexpr int kRing = 8;  // ring slots per thread: column p is read while p+1..p+7 are in flight
+// Bulk loads fill the same ring as kStages stages of kStageCols columns: one
+// tensor copy per field and stage ({T rows, kStageCols columns} box).
+constexpr int kStageCols = 4, kStages = kRing / kStageCols;
+static_assert(kStageCols == TMAP_BOX_COLS, "bulk-load box width");
 
 // 4-byte async copy to shared address `d` (a 32-bit shared-window address);
 // pred == false zero-fills without reading (src stays a valid address).
@@ -57,6 +61,42 @@ __device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_gro
 template <int N>
 __device__ __forceinline__ void cpa_wait() {
     asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// ---- bulk tensor loads (TMA) completed on an mbarrier per ring slot
+__device__ int g_march_tma_error;  // set when a bulk-load wait ran out of iterations
+
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity) {
+    unsigned done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+// Waits for phase `parity` of the barrier, at most kWaitIters tries.
+constexpr int kWaitIters = 1 << 20;
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned parity) {
+    for (int i = 0; i < kWaitIters; i++)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+// One box ({T rows, kStageCols columns}, as encoded in the map) of a 2-D
+// tensor {nz, nx} into shared memory, columns consecutive; row z0 must be a
+// multiple of 4 (16-byte aligned); coordinates outside the tensor read as zero.
+__device__ __forceinline__ void tma_col(unsigned dst, const void *tmap, int z0, int col, unsigned bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+        "[%4];" ::"r"(dst),
+        "l"(tmap), "r"(z0), "r"(col), "r"(bar)
+        : "memory");
 }
 
 // Words staged per column step: stress at p (NS), velocity, displacement and
@@ -74,13 +114,20 @@ __host__ __device__ constexpr int march_smem_words(int threads) {
     return (kRing * MarchWords<PSV>::N + 2 * ((PSV ? 2 : 1) + (PSV ? 2 : 1))) * threads + 2 * 2 * (2 + 2) * 2;
 }
 
-template <bool PSV>
+// TMA = false: each thread stages its own row with 4-byte cp.async.
+// TMA = true: warp 0 loads whole strip columns with bulk tensor copies (one
+// per field and 32 rows) that complete on the ring slot's mbarrier; needs
+// nz % 4 == 0 and the slots' tensor maps. Both read the same values for
+// every cell they use, so results are identical.
+template <bool PSV, bool TMA>
 __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restrict__ slots, int kstep,
                                                             int chunk) {
     using W = MarchWords<PSV>;
     constexpr int NS = W::NS, NV = W::NV;
     constexpr int NZS = PSV ? 2 : 1;  // stress components with a z-derivative (sxz, szz | szy)
-    extern __shared__ float smem[];
+    extern __shared__ __align__(128) float smem[];
+    __shared__ __align__(8) unsigned long long s_bar[kStages];
+    __shared__ int s_dead;
     const int T = blockDim.x, O = T - 8;
     const int TP = T + 4;  // exchange rows padded by 2 on both sides
     float *ring = smem;                                  // [kRing][W::N][T]
@@ -193,6 +240,72 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
         if (PSV) cpa4(rs + W::LAM * T * 4, lam + km, cm);
     };
 
+    const int p_first = c0 - 3, p_last = c1 + 2;
+    const int nstep = p_last - p_first + 1;
+    const int nstage = (nstep + kStageCols - 1) / kStageCols;
+    // bulk loads (warp 0; lane 0 arms the stage's barrier with the byte count first)
+    const char *tm = static_cast<const char *>(S.tmap);
+    const int w0 = strip * O - 4;
+    const unsigned bar0 = (unsigned)__cvta_generic_to_shared(s_bar);
+    const unsigned ring0 = (unsigned)__cvta_generic_to_shared(ring);
+    constexpr int NTF = NS + 2 * NV + 2 + (PSV ? 1 : 0);  // fields per column step
+    // lane f < NTF of warp 0 loads field f: its ring word, tensor map and
+    // column offset from the step's column p (stress p, velocity,
+    // displacement and 1/rho p-1, moduli p-3)
+    int lw = 0, lcol = 0;
+    const void *lmap = tm;
+    if (TMA && t < NTF) {
+        int map;
+        if (t < NS) {
+            lw = W::SG + t;
+            map = PSV ? SXX0 + 2 * t + par : TMAP_SH + SXY0 + 2 * t + par;
+        } else if (t < NS + NV) {
+            lw = W::V + (t - NS);
+            map = PSV ? VX0 + 2 * (t - NS) + par : TMAP_SH + VY0 + par;
+            lcol = -1;
+        } else if (t < NS + 2 * NV) {
+            lw = W::U + (t - NS - NV);
+            map = PSV ? UX + (t - NS - NV) : TMAP_SH + UY;
+            lcol = -1;
+        } else if (t == NS + 2 * NV) {
+            lw = W::RHO;
+            map = TMAP_RINV;
+            lcol = -1;
+        } else if (t == NS + 2 * NV + 1) {
+            lw = W::MU;
+            map = TMAP_MU;
+            lcol = -3;
+        } else {
+            lw = PSV ? W::LAM : W::MU;
+            map = TMAP_LAM;
+            lcol = -3;
+        }
+        lmap = tm + (size_t)map * TMAP_BYTES;
+    }
+    // stage m = column steps [kStageCols*m, kStageCols*(m+1)) into ring stage m % kStages
+    auto issue_tma = [&](int m) {
+        if (t >= 32) return;
+        const int slot = m % kStages;
+        const unsigned bar = bar0 + 8u * (unsigned)slot;
+        if (t == 0) mbar_expect_tx(bar, (unsigned)(NTF * T * kStageCols * 4));
+        __syncwarp();
+        if (t < NTF) {
+            // the stage was last read by ordinary loads (before a block barrier)
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            const unsigned dst = ring0 + 4u * (unsigned)((slot * W::N + lw) * kStageCols * T);
+            tma_col(dst, lmap, w0, p_first + kStageCols * m + lcol, bar);
+        }
+    };
+    bool dead = false;  // a bulk-load wait ran out of iterations (never in a correct run)
+    if (TMA) {
+        if (t == 0) {
+            for (int sl = 0; sl < kStages; sl++) mbar_init(bar0 + 8u * (unsigned)sl, 1);
+            s_dead = 0;
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+        __syncthreads();
+    }
+
     float sq[4][NS], vq[4][NV], dzq[3][NV];
 #pragma unroll
     for (int a = 0; a < 4; a++) {
@@ -206,13 +319,19 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
 #pragma unroll
         for (int f = 0; f < NV; f++) dzq[a][f] = 0.f;
 
-    const int p_first = c0 - 3, p_last = c1 + 2;
-    const int nstep = p_last - p_first + 1;
-    // prologue: kRing - 1 column steps in flight
+    int issued = 0, sdone = 0;  // stages issued / waited for (bulk loads)
+    // prologue: kRing - 1 column steps (cp.async) or kStages stages (bulk) in flight
+    if (TMA) {
+        for (int m = 0; m < kStages && m < nstage; m++) {
+            issue_tma(m);
+            issued = m + 1;
+        }
+    } else {
 #pragma unroll
-    for (int q = 0; q < kRing - 1; q++) {
-        if (q < nstep) issue(p_first + q, q);
-        cpa_commit();
+        for (int q = 0; q < kRing - 1; q++) {
+            if (q < nstep) issue(p_first + q, q);
+            cpa_commit();
+        }
     }
     // P-SV: unrolled by the queue depth, so the register queues rotate by
     // renaming (fewer registers and moves); SH keeps the rolled loop, which
@@ -221,14 +340,37 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
 #pragma unroll kUnroll
     for (int q = 0; q < nstep; q++) {
         const int p = p_first + q;
-        cpa_wait<kRing - 2>();  // column step q has landed (own row)
-        const float *rs = ring + (q % kRing) * W::N * T + t;
         float cur[W::N];
+        if (TMA) {
+            const int m = q / kStageCols, qc = q - m * kStageCols;
+            if (qc == 0) {
+                // stage m has landed (whole strip, kStageCols columns): phase m / kStages of its barrier
+                if (!dead && !mbar_wait_bounded(bar0 + 8u * (unsigned)(m % kStages), (unsigned)((m / kStages) & 1))) {
+                    dead = true;
+                    s_dead = 1;
+                    atomicOr(&g_march_tma_error, 1);
+                }
+                sdone = m + 1;
+                // refill the stage consumed in stage m-1 (every thread finished
+                // reading it before the previous column step's barrier)
+                if (m >= 1 && m + 1 < nstage && !dead) {
+                    issue_tma(m + 1);
+                    issued = m + 2;
+                }
+            }
+            const float *rs = ring + ((m % kStages) * W::N * kStageCols + qc) * T + t;
 #pragma unroll
-        for (int w = 0; w < W::N; w++) cur[w] = rs[w * T];
-        // refill the slot read at the previous step
-        if (q + kRing - 1 < nstep) issue(p + kRing - 1, (q + kRing - 1) % kRing);
-        cpa_commit();
+            for (int w = 0; w < W::N; w++) cur[w] = rs[w * kStageCols * T];
+        } else {
+            cpa_wait<kRing - 2>();  // column step q has landed (own row)
+            const float *rs = ring + (q % kRing) * W::N * T + t;
+#pragma unroll
+            for (int w = 0; w < W::N; w++) cur[w] = rs[w * T];
+            // refill the slot read at the previous step (every thread finished
+            // reading it before the previous step's barrier)
+            if (q + kRing - 1 < nstep) issue(p + kRing - 1, (q + kRing - 1) % kRing);
+            cpa_commit();
+        }
 
         const int buf = q & 1;
 #pragma unroll
@@ -287,7 +429,7 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
                 inj_next = inj_ptr < inj_end ? inj_local[inj_ptr] : 0x7fffffff;
             }
             if ((unsigned)pv < (unsigned)nx && rowin) {
-                const float ab = cur[W::AX] * azj;
+                const float ab = (TMA ? __ldg(ax + pv) : cur[W::AX]) * azj;
                 const float rinv = cur[W::RHO];
 #pragma unroll
                 for (int f = 0; f < NV; f++) vn[f] = st_velocity(ab, dt, ds[f], rinv, cur[W::V + f]);
@@ -333,6 +475,7 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
             vz_w[f * TP + st] = vn[f];
         }
         __syncthreads();
+        if (TMA && s_dead) break;  // uniform: s_dead is read after the barrier
         // z-gradient of the new velocity at column pv
 #pragma unroll
         for (int f = 0; f < NV; f++) {
@@ -366,28 +509,52 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
             }
         }
     }
-    cpa_wait<0>();
+    if (!TMA) cpa_wait<0>();
+    if (TMA && s_dead) {
+        // leave no bulk copy in flight into this block's shared memory
+        for (int mm = sdone; mm < issued; mm++)
+            (void)mbar_wait_bounded(bar0 + 8u * (unsigned)(mm % kStages), (unsigned)((mm / kStages) & 1));
+    }
 }
 
-cudaError_t launch_march(bool psv, int threads, int chunk, const Slot *d_slots, int nslots, int max_tiles, int k,
-                         cudaStream_t st) {
+int march_tma_error() {
+    int e = 0;
+    if (cudaMemcpyFromSymbol(&e, g_march_tma_error, sizeof(int)) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return 1;
+    }
+    if (e) {
+        const int z = 0;
+        (void)cudaMemcpyToSymbol(g_march_tma_error, &z, sizeof(int));
+    }
+    return e;
+}
+
+template <bool PSV, bool TMA>
+static cudaError_t launch_march_t(dim3 grid, int threads, size_t smem, const Slot *d_slots, int k, int chunk,
+                                  cudaStream_t st) {
+    static bool attr_set = false;
+    if (!attr_set) {
+        const cudaError_t e = cudaFuncSetAttribute(k_march<PSV, TMA>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   march_smem_words<PSV>(kMaxMarchThreads) * 4);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    k_march<PSV, TMA><<<grid, threads, smem, st>>>(d_slots, k, chunk);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_march(bool psv, bool tma, int threads, int chunk, const Slot *d_slots, int nslots, int max_tiles,
+                         int k, cudaStream_t st) {
     if (nslots <= 0 || max_tiles <= 0) return cudaSuccess;
     if (threads < 32 || threads > kMaxMarchThreads || threads % 32 || chunk < 1) return cudaErrorInvalidValue;
-    dim3 grid(max_tiles, nslots);
-    static bool attr_set[2] = {false, false};
-    const int maxw = psv ? march_smem_words<true>(kMaxMarchThreads) : march_smem_words<false>(kMaxMarchThreads);
-    if (!attr_set[psv]) {
-        cudaError_t e = psv ? cudaFuncSetAttribute(k_march<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxw * 4)
-                            : cudaFuncSetAttribute(k_march<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxw * 4);
-        if (e != cudaSuccess) return e;
-        attr_set[psv] = true;
-    }
+    const dim3 grid(max_tiles, nslots);
     const size_t smem = (size_t)(psv ? march_smem_words<true>(threads) : march_smem_words<false>(threads)) * 4;
     if (psv)
-        k_march<true><<<grid, threads, smem, st>>>(d_slots, k, chunk);
-    else
-        k_march<false><<<grid, threads, smem, st>>>(d_slots, k, chunk);
-    return cudaGetLastError();
+        return tma ? launch_march_t<true, true>(grid, threads, smem, d_slots, k, chunk, st)
+                   : launch_march_t<true, false>(grid, threads, smem, d_slots, k, chunk, st);
+    return tma ? launch_march_t<false, true>(grid, threads, smem, d_slots, k, chunk, st)
+               : launch_march_t<false, false>(grid, threads, smem, d_slots, k, chunk, st);
 }
 
 }  // namespace gb

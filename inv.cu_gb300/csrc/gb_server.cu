@@ -430,7 +430,7 @@ int round_once(Server &S, std::vector<Req *> &act) {
                 GB_CUDA_TRY(launch_ckpt_store(tab, cnt, (int)max_n_fwd[w], k, 1, w, S.st));
                 S.launches += q16 ? 2 : 1;
             }
-            GB_CUDA_TRY(launch_step(w, kSrvTile, tab, cnt, max_tiles[w], k, S.st));
+            GB_CUDA_TRY(launch_step(w, kSrvTile, tab, cnt, max_tiles[w], k, false, S.st));
             S.launches++;
             if (k == S.sfe - 1 && cnt > nadj) {
                 if (q16) GB_CUDA_TRY(launch_ckpt_amax(tab, cnt, (int)max_n_fwd[w], k, 0, w, S.st));

@@ -7,6 +7,8 @@
 // captured once into a CUDA graph per (pass kind, n) and replayed; the
 // per-slot descriptors live in device memory so a replay can serve another
 // set of shots after one small host-to-device copy.
+#include <cuda.h>  // CUtensorMap and its enums (the encoder comes from the runtime's driver entry point)
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -170,6 +172,7 @@ int Solver::init(const Config &cfg, int nx_, int nz_, float xmax_, float zmax_) 
     if (cfg.has("graphs")) opt_graphs = cfg.iv("graphs") != 0;
     if (cfg.has("ckpt_precision")) opt_ckpt = cfg.iv("ckpt_precision");
     if (cfg.has("tile")) opt_tile = cfg.iv("tile");
+    if (cfg.has("tma")) opt_tma = cfg.iv("tma") != 0;
     if (cfg.has("cluster")) opt_cluster = std::max(0, std::min(16, cfg.iv("cluster")));
     nx = nx_;
     nz = nz_;
@@ -278,6 +281,7 @@ void Solver::release() {
         }
         cudaFree(b.ckpt);
         cudaFree(b.amax);
+        cudaFree(b.tmaps);
     }
     slots.clear();
     for (float *p : {lambda, mu, rho, rinv, k_lambda, k_mu, k_rho, stf[0], stf[1], stf[2], ax, az}) cudaFree(p);
@@ -390,6 +394,90 @@ size_t Solver::slot_bytes(int prec) const {
     return b;
 }
 
+// cuTensorMapEncodeTiled through the runtime (no link against the driver
+// library); null when the driver does not offer it.
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        else
+            (void)cudaGetLastError();
+    }
+    return fn;
+}
+
+// One field float[nx*nz] (k = i*nz + j) as a 2-D tensor {nz, nx}: a box is
+// `rows` consecutive rows of TMAP_BOX_COLS consecutive columns, zero outside
+// the grid.
+static bool encode_field_map(void *out, const float *base, int nx, int nz, int rows) {
+    const auto enc = tensor_map_encoder();
+    if (!enc || !base || (reinterpret_cast<uintptr_t>(base) & 15) || nz % 4 || rows < 1 || rows > 256 || rows % 4)
+        return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)nz, (cuuint64_t)nx};
+    const cuuint64_t strides[1] = {(cuuint64_t)nz * 4};
+    const cuuint32_t box[2] = {(cuuint32_t)rows, (cuuint32_t)TMAP_BOX_COLS};
+    const cuuint32_t estr[2] = {1, 1};
+    return enc(static_cast<CUtensorMap *>(out), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(base), dims,
+               strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Encodes the TMAP_N maps of a slot's state fields and the model for a box
+// of `rows` rows; false when a field cannot be described.
+static bool encode_slot_maps(std::vector<CUtensorMap> &h, const float *state, bool sh, bool psv, const float *rinv,
+                             const float *mu, const float *lambda, int nx, int nz, int rows) {
+    static_assert(sizeof(CUtensorMap) == TMAP_BYTES, "tensor map size");
+    h.assign(TMAP_N, CUtensorMap{});
+    const size_t nc = (size_t)nx * nz;
+    bool ok = true;
+    const float *p = state;
+    if (sh)
+        for (int f = 0; f < NSH; f++) ok = ok && encode_field_map(&h[TMAP_SH + f], p + (size_t)f * nc, nx, nz, rows);
+    if (sh) p += (size_t)NSH * nc;
+    if (psv)
+        for (int f = 0; f < NPSV; f++) ok = ok && encode_field_map(&h[f], p + (size_t)f * nc, nx, nz, rows);
+    return ok && encode_field_map(&h[TMAP_RINV], rinv, nx, nz, rows) &&
+           encode_field_map(&h[TMAP_MU], mu, nx, nz, rows) && encode_field_map(&h[TMAP_LAM], lambda, nx, nz, rows);
+}
+
+// Space for a slot's tensor maps, for the marching kernel's bulk loads;
+// tma_ok records whether its fields can be described (nz % 4 == 0, aligned
+// buffers, driver support). The maps are encoded by refresh_tmaps.
+int Solver::build_tmaps(SlotBuf &b) {
+    std::vector<CUtensorMap> h;
+    if (!(nz % 4 == 0 && encode_slot_maps(h, b.state, sh, psv, rinv, mu, lambda, nx, nz, 32))) {
+        tma_ok = false;
+        return GB_OK;
+    }
+    GB_CUDA_TRY(cudaMalloc(&b.tmaps, sizeof(CUtensorMap) * TMAP_N));
+    tmaps_T = 0;
+    return GB_OK;
+}
+
+// Encodes every slot's maps for marching blocks of `threads` rows (the box
+// height), ordered on the solver's stream after the kernels that read the
+// previous ones. A no-op when they are current or bulk loads are off.
+int Solver::refresh_tmaps(int threads) {
+    if (!use_tma() || threads <= 0 || threads == tmaps_T) return GB_OK;
+    std::vector<CUtensorMap> h;
+    for (auto &b : slots) {
+        if (!b.tmaps || !encode_slot_maps(h, b.state, sh, psv, rinv, mu, lambda, nx, nz, threads)) {
+            set_error("tensor maps: a field cannot be described for bulk loads");
+            return GB_ERR_STATE;
+        }
+        GB_CUDA_TRY(cudaMemcpyAsync(b.tmaps, h.data(), sizeof(CUtensorMap) * TMAP_N, cudaMemcpyHostToDevice, st));
+    }
+    tmaps_T = threads;
+    return GB_OK;
+}
+
 int Solver::ensure_slots(int n) {
     if (capacity == 0) {
         size_t freeb = 0, totalb = 0;
@@ -433,6 +521,9 @@ int Solver::ensure_slots(int n) {
                 GB_CUDA_TRY(cudaMemset(b.adstf[c], 0, tr * 4));
             }
         }
+        if (slots.empty()) tma_ok = true;  // until a slot's maps fail
+        int rc = build_tmaps(b);
+        if (rc) return rc;
         slots.push_back(b);
     }
     if (adj && nsfe) {
@@ -525,6 +616,7 @@ int Solver::fill_slots(int kind, const int *shots, int n, bool record_u) {
         }
         if (psv)
             for (int f = 0; f < NPSV; f++) S.psv[f] = p + (size_t)f * nc;
+        S.tmap = tma_ok ? B.tmaps : nullptr;
         S.it_base = 0;
         S.par0 = 0;
         S.pts_i = d_rec_cells;
@@ -613,8 +705,8 @@ int Solver::enqueue_pass(int kind, int n, bool snapshot, int snap_isrc) {
             }
         }
         if (it == w0 && win_steps > 0) GB_CUDA_TRY(record_timing(ev_win0));
-        if (sh) GB_CUDA_TRY(launch_step(false, tile, ds, n, max_tiles(), it, st));
-        if (psv) GB_CUDA_TRY(launch_step(true, tile, ds, n, max_tiles(), it, st));
+        if (sh) GB_CUDA_TRY(launch_step(false, tile, ds, n, max_tiles(), it, use_tma(), st));
+        if (psv) GB_CUDA_TRY(launch_step(true, tile, ds, n, max_tiles(), it, use_tma(), st));
         stats.launches += nwave;
         if (it + 1 == w1 && win_steps > 0) GB_CUDA_TRY(record_timing(ev_win1));
         par ^= 1;
@@ -662,15 +754,23 @@ int Solver::autotune(int n) {
             tmp[b].tiles_x = (nx + tc.tx - 1) / tc.tx;
         }
         GB_CUDA_TRY(cudaMemcpyAsync(d_tune, tmp.data(), sizeof(Slot) * capacity, cudaMemcpyHostToDevice, st));
+        if (tc.threads) {
+            const int rc = refresh_tmaps(tc.threads);
+            if (rc) return rc;
+        }
         const int mt = ((nz + tc.tz - 1) / tc.tz) * ((nx + tc.tx - 1) / tc.tx);
         const int reps = 8;
         for (int r = 0; r < 3 + reps; r++) {
             if (r == 3) GB_CUDA_TRY(cudaEventRecord(ev_win0, st));
-            if (sh) GB_CUDA_TRY(launch_step(false, tc, d_tune, n, mt, r, st));
-            if (psv) GB_CUDA_TRY(launch_step(true, tc, d_tune, n, mt, r, st));
+            if (sh) GB_CUDA_TRY(launch_step(false, tc, d_tune, n, mt, r, use_tma(), st));
+            if (psv) GB_CUDA_TRY(launch_step(true, tc, d_tune, n, mt, r, use_tma(), st));
         }
         GB_CUDA_TRY(cudaEventRecord(ev_win1, st));
         GB_CUDA_TRY(cudaEventSynchronize(ev_win1));
+        if (tc.threads && use_tma() && march_tma_error()) {
+            set_error("marching kernel: a bulk-load wait ran out of iterations while tuning");
+            return GB_ERR_CUDA;
+        }
         float ms = 0;
         GB_CUDA_TRY(cudaEventElapsedTime(&ms, ev_win0, ev_win1));
         if (ms < best) {
@@ -684,6 +784,10 @@ int Solver::autotune(int n) {
 }
 
 int Solver::run_pass(int kind, int n, bool snapshot, int snap_isrc) {
+    if (tile.threads) {
+        const int rc = refresh_tmaps(tile.threads);
+        if (rc) return rc;
+    }
     GB_CUDA_TRY(cudaEventRecord(ev_pass0, st));
     GB_CUDA_TRY(launch_reciprocal(rinv, rho, ncell(), st));
     if (opt_graphs && !snapshot) {
@@ -721,6 +825,11 @@ int Solver::run_pass(int kind, int n, bool snapshot, int snap_isrc) {
     }
     GB_CUDA_TRY(cudaEventRecord(ev_pass1, st));
     GB_CUDA_TRY(cudaStreamSynchronize(st));
+    if (tile.threads) stats.march_bulk = use_tma() ? 1 : 0;
+    if (use_tma() && tile.threads && march_tma_error()) {
+        set_error("marching kernel: a bulk-load wait ran out of iterations; the pass is invalid");
+        return GB_ERR_CUDA;
+    }
     float ms = 0;
     GB_CUDA_TRY(cudaEventElapsedTime(&ms, ev_pass0, ev_pass1));
     if (kind == PASS_ADJ)

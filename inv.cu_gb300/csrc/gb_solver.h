@@ -23,6 +23,7 @@ struct SlotBuf {
     void *ckpt = nullptr;
     float *amax = nullptr;
     int ckpt_prec = -1;
+    void *tmaps = nullptr;  // TMAP_N tensor maps of this slot's fields and the model (device)
 };
 
 struct PointSet {
@@ -59,6 +60,12 @@ struct Solver {
     int opt_ckpt = CKPT_F32;
     int opt_tile = 0;  // 0 = autotune
     double opt_budget_gb = 0;
+    int opt_tma = 1;      // marching kernel loads columns with bulk tensor copies when possible
+    bool tma_ok = false;  // every slot has its tensor maps (nz % 4 == 0, aligned buffers)
+    bool use_tma() const { return opt_tma && tma_ok; }
+    int tmaps_T = 0;      // box height the slots' maps are encoded for (0: stale)
+    int build_tmaps(SlotBuf &b);
+    int refresh_tmaps(int threads);
     int opt_cluster = 1;  // cluster-resident passes: 0 never, 1 automatic R, 2..16 this cluster size
 
     // device buffers in the reference layout

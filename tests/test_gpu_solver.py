@@ -125,6 +125,42 @@ def test_kernel_configurations_give_identical_results(gpu, orc, tile, wave):
         np.testing.assert_array_equal(k[name], ref_k[name])
 
 
+@pytest.mark.parametrize("wave", ["psv", "sh"])
+@pytest.mark.parametrize("tile", [6, 8, 10, 13, 15, 17, 19, 20])
+def test_march_bulk_loads_identical_to_cp_async(gpu, orc, tile, wave):
+    """The marching kernel's bulk tensor loads (nz % 4 == 0) and its per-row
+    cp.async staging give the same bits, and match the 2-D tile kernel."""
+    case = cases.make_case(wave=wave, nx=133, nz=76, nt=250, nsrc=2, nrec=25, seed=29)
+    rng = np.random.default_rng(7)
+    ad = {c: (rng.standard_normal((case["nrec"], case["nt"])) * 1e-3).astype(np.float32) for c in "xyz"}
+
+    def run(t, tma):
+        cfg, sol = cases.gpu_solver(gpu, case)
+        sol.set_option("cluster", 0)
+        sol.set_option("tma", tma)
+        sol.set_option("tile", t)
+        sol.run_forward_batch([0, 1])
+        bulk = sol.stats().march_bulk
+        tr = {c: sol.out(c, slot=1) for c in comps(wave)}
+        for c in comps(wave):
+            sol.set_adstf(c, ad[c], slot=0)
+            sol.set_adstf(c, ad[c], slot=1)
+        sol.initKernels()
+        sol.run_adjoint_batch([0, 1])
+        return tr, sol.kernels(), bulk
+
+    tr_b, k_b, bulk_b = run(tile, 1)
+    tr_c, k_c, bulk_c = run(tile, 0)
+    tr_t, k_t, _ = run(1, 1)
+    assert bulk_b == 1 and bulk_c == 0
+    for c in comps(wave):
+        np.testing.assert_array_equal(tr_b[c], tr_c[c])
+        np.testing.assert_array_equal(tr_b[c], tr_t[c])
+    for name in kernel_names(wave):
+        np.testing.assert_array_equal(k_b[name], k_c[name])
+        np.testing.assert_array_equal(k_b[name], k_t[name])
+
+
 def test_graphs_and_eager_identical(gpu, orc):
     case = cases.make_case(wave="sh", nx=100, nz=64, nt=300, nsrc=2, nrec=20, seed=19)
     cfg, a = cases.gpu_solver(gpu, case)
