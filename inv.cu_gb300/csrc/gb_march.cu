@@ -336,7 +336,7 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
     // P-SV: unrolled by the queue depth, so the register queues rotate by
     // renaming (fewer registers and moves); SH keeps the rolled loop, which
     // fits its registers better
-    constexpr int kUnroll = PSV ? 4 : 1;
+    constexpr int kUnroll = (PSV || TMA) ? 4 : 1;
 #pragma unroll kUnroll
     for (int q = 0; q < nstep; q++) {
         const int p = p_first + q;
