@@ -221,6 +221,13 @@ int Solver::init(const Config &cfg, int nx_, int nz_, float xmax_, float zmax_) 
     for (cudaEvent_t *e : {&ev_pass0, &ev_pass1, &ev_win0, &ev_win1}) GB_CUDA_TRY(cudaEventCreate(e));
 
     const size_t n = ncell();
+    {
+        int dev = 0, sms = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && sms > 0)
+            num_sms = sms;
+        (void)cudaGetLastError();
+    }
     GB_CUDA_TRY(cudaMalloc(&lambda, n * 4));
     GB_CUDA_TRY(cudaMalloc(&mu, n * 4));
     GB_CUDA_TRY(cudaMalloc(&rho, n * 4));
@@ -879,12 +886,24 @@ bool Solver::cluster_geometry(bool wave_psv, int n, ClusterGeom *out) const {
             g.nrec_cta = *std::max_element(per.begin(), per.end());
             if (cluster_smem_bytes(wave_psv, g, nz) > limit) continue;
             const int occ = cluster_occupancy(wave_psv, g, nz);
+            if (occ < 1) {
+                if (trace)
+                    std::fprintf(stderr, "gbfwi cluster %s R=%d cols=%d qmax=%d threads=%d smem=%zu: no fit\n",
+                                 wave_psv ? "psv" : "sh", R, g.cols_per, g.qmax, g.G * nz,
+                                 cluster_smem_bytes(wave_psv, g, nz));
+                continue;
+            }
+            // per-step time ~ cells per SM (CTAs sharing an SM add up) plus a
+            // barrier allowance, times the rounds the batch needs
+            const int resident = std::min(n, occ);
+            const int per_sm = (R * resident + num_sms - 1) / num_sms;
+            const double cost =
+                (double)((n + occ - 1) / occ) * ((double)std::max(per_sm, 1) * g.cols_per * nz + 6000.0);
             if (trace)
-                std::fprintf(stderr, "gbfwi cluster %s R=%d cols=%d qmax=%d threads=%d smem=%zu clusters=%d\n",
+                std::fprintf(stderr,
+                             "gbfwi cluster %s R=%d cols=%d qmax=%d threads=%d smem=%zu clusters=%d cost=%.0f\n",
                              wave_psv ? "psv" : "sh", R, g.cols_per, g.qmax, g.G * nz,
-                             cluster_smem_bytes(wave_psv, g, nz), occ);
-            if (occ < 1) continue;
-            const double cost = (double)((n + occ - 1) / occ) * ((double)g.cols_per * nz + 6000.0);
+                             cluster_smem_bytes(wave_psv, g, nz), occ, cost);
             if (best < 0 || cost < best) {
                 best = cost;
                 *out = g;

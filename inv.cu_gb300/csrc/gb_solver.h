@@ -60,6 +60,7 @@ struct Solver {
     int opt_ckpt = CKPT_F32;
     int opt_tile = 0;  // 0 = autotune
     double opt_budget_gb = 0;
+    int num_sms = 152;    // streaming multiprocessors of the device (queried at init)
     int opt_tma = 1;      // marching kernel loads columns with bulk tensor copies when possible
     bool tma_ok = false;  // every slot has its tensor maps (nz % 4 == 0, aligned buffers)
     bool use_tma() const { return opt_tma && tma_ok; }
