@@ -139,7 +139,9 @@ int gb_solver_batch_capacity(gb_solver *s);
  * state fits in their shared memory, with the cluster size chosen by
  * occupancy; 2..16: that cluster size; 0: never), "tma" (1: the marching
  * kernel loads grid columns with bulk tensor copies when nz % 4 == 0,
- * default; 0: per-thread cp.async), "hbm_budget_gb". Options
+ * default; 0: per-thread cp.async), "cluster_stage" (1: a cluster adjoint
+ * stages each checkpoint in shared memory before the kernel accumulation when
+ * it fits, default; 0: reads it from HBM), "hbm_budget_gb". Options
  * change no forward result; "ckpt" changes kernels by the checkpoint
  * rounding and "cluster" by the order in which shots are summed. */
 int gb_solver_set_option(gb_solver *s, const char *key, double value);

@@ -305,6 +305,8 @@ int gb_solver_set_option(gb_solver *s, const char *key, double value) {
             v.tuned = false;
         }
         v.invalidate_graphs();
+    } else if (k == "cluster_stage") {
+        v.opt_stage = value != 0;
     } else if (k == "tma") {
         v.opt_tma = value != 0;
         v.invalidate_graphs();

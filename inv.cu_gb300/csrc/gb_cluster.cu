@@ -67,6 +67,12 @@ __device__ __forceinline__ void cp_async4(float *dst, const float *src) {
                  : "memory");
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+// as cp_async4, zero-filling dst without reading when pred is false (src stays valid)
+__device__ __forceinline__ void cp_async4_zf(float *dst, const float *src, bool pred) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+                 "l"(src), "r"(pred ? 4 : 0)
+                 : "memory");
+}
 
 __device__ __forceinline__ float ck_get(const Slot &S, int isfe, int q, size_t k, size_t n, float inv) {
     const size_t off = ((size_t)isfe * S.nf + q) * n + k;
@@ -121,6 +127,10 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
     // step's forward source
     float *rbuf = reinterpret_cast<float *>(rtab + g.nrec_cta);
     float *sbuf = rbuf + (size_t)g.nrec_cta * NV;
+    // adjoint with g.stage: the checkpoint the next kernel accumulation reads,
+    // NV displacement fields over columns -1 .. cp+1 and NV velocity fields
+    // over columns 0 .. cp-1, stored by columns ([field][column][row])
+    float *ckst = sbuf + NV;
     __shared__ int s_count;
     int *map = reinterpret_cast<int *>(sm);
     for (int e = t; e < cp * nz; e += blockDim.x) map[e] = -1;
@@ -208,6 +218,26 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
                 const size_t ks = (size_t)rtab[e] * nt + step;
 #pragma unroll
                 for (int f = 0; f < NV; f++) cp_async4(rbuf + e * NV + f, inj_of(f) + ks);
+            }
+        }
+    };
+    // copies checkpoint isfe into ckst (this thread: row j of the columns
+    // grp, grp + G, ...); completed by cp_async_wait_all
+    auto stage_ckpt = [&](int isfe) {
+        const float *ckb = static_cast<const float *>(S.ckpt) + ((size_t)isfe * S.nf + base_ck) * ncell + j;
+#pragma unroll
+        for (int f = 0; f < NV; f++) {
+            for (int col = grp; col < cp + 3; col += g.G) {
+                const int gc = x0 - 1 + col;
+                const bool ok = gc >= 0 && gc < nx;
+                cp_async4_zf(ckst + ((size_t)f * (cp + 3) + col) * nz + j, ckb + (size_t)f * ncell + (size_t)(ok ? gc : 0) * nz,
+                             ok);
+            }
+            for (int col = grp; col < cp; col += g.G) {
+                const int gc = x0 + col;
+                const bool ok = gc < nx;
+                cp_async4_zf(ckst + ((size_t)NV * (cp + 3) + (size_t)f * cp + col) * nz + j,
+                             ckb + (size_t)(NV + f) * ncell + (size_t)(ok ? gc : 0) * nz, ok);
             }
         }
     };
@@ -335,6 +365,7 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
             if (isfe_n >= 0) store_ckpt(isfe_n, FU, 0);
         }
         prefetch(it + 1);
+        if (ADJ && g.stage && S.ckpt && S.sfe > 0 && it % S.sfe == 0 && it / S.sfe < S.nsfe) stage_ckpt(it / S.sfe);
         // ---- phase B: velocity gradients and stress update
         {
             float wb[NV][4];  // x-window: columns c-1, c, c+1, c+2
@@ -403,17 +434,33 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
             const int zm = zv ? -1 : 0, zp = zv ? 1 : 0, zp2 = zv ? 2 : 0;
             auto colk = [&](int q) -> size_t { return (size_t)min(max(i0 + q, 0), nx - 1) * nz + j; };
             float cw[NV][4];  // checkpointed displacement f at columns c-1, c, c+1, c+2
+            if (g.stage) {
+                cp_async_wait_all();
+                __syncthreads();
+            }
 #pragma unroll
             for (int f = 0; f < NV; f++) {
-                const float *u = ckb + (size_t)f * ncell;
-                cw[f][0] = __ldg(u + colk(-1));
-                cw[f][1] = __ldg(u + colk(0));
-                cw[f][2] = __ldg(u + colk(1));
+                if (g.stage) {
+                    const float *us = ckst + ((size_t)f * (cp + 3) + cb + 1) * nz + j;
+                    cw[f][0] = us[-(int)nz];
+                    cw[f][1] = us[0];
+                    cw[f][2] = us[nz];
+                } else {
+                    const float *u = ckb + (size_t)f * ncell;
+                    cw[f][0] = __ldg(u + colk(-1));
+                    cw[f][1] = __ldg(u + colk(0));
+                    cw[f][2] = __ldg(u + colk(1));
+                }
             }
             float *kl = kpart + ((size_t)slot * 3 + 0) * ncell + kc;
             float *km = kpart + ((size_t)slot * 3 + 1) * ncell + kc;
             float *kr = kpart + ((size_t)slot * 3 + 2) * ncell + kc;
-#pragma unroll 1
+            const bool staged = g.stage != 0;  // staging copies waited for above
+            // staged checkpoint: displacement f at local column c + o (o >= -1), velocity f at c
+            const float *su = ckst + (size_t)(cb + 1) * nz + j;
+            const float *sv = ckst + ((size_t)NV * (cp + 3) + cb) * nz + j;
+            // four columns per iteration keep their kernel-buffer loads in flight together
+#pragma unroll 4
             for (int q = 0; q < QM; q++) {
                 if (q < nq) {
                     const bool gx = (xv_mask >> q) & 1;
@@ -421,15 +468,27 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
 #pragma unroll
                     for (int f = 0; f < NV; f++) {
                         const float *u = ckb + (size_t)f * ncell;
-                        cw[f][3] = __ldg(u + colk(q + 2));
                         const float *uc = u + kc + (size_t)q * nz;
-                        vf[f] = __ldg(uc + (size_t)NV * ncell);  // checkpointed velocity f
+                        const float *us = su + ((size_t)f * (cp + 3) + q) * nz;
+                        float z1, z2, zm1;
+                        if (staged) {
+                            cw[f][3] = us[2 * nz];
+                            vf[f] = sv[((size_t)f * cp + q) * nz];
+                            z1 = us[zp];
+                            z2 = us[zp2];
+                            zm1 = us[zm];
+                        } else {
+                            cw[f][3] = __ldg(u + colk(q + 2));
+                            vf[f] = __ldg(uc + (size_t)NV * ncell);  // checkpointed velocity f
+                            z1 = __ldg(uc + zp);
+                            z2 = __ldg(uc + zp2);
+                            zm1 = __ldg(uc + zm);
+                        }
                         const float *u0 = P + (FU + f) * fs + q;
                         ux[f] = gx ? st_dplus(u0[1], u0[0], u0[2], u0[-1], c9x, c24x) : 0.f;
                         uzz[f] = zv ? st_dplus(u0[rs], u0[0], u0[2 * rs], u0[-rs], c9z, c24z) : 0.f;
                         fx[f] = gx ? st_dplus(cw[f][2], cw[f][1], cw[f][3], cw[f][0], c9x, c24x) : 0.f;
-                        fz[f] = zv ? st_dplus(__ldg(uc + zp), cw[f][1], __ldg(uc + zp2), __ldg(uc + zm), c9z, c24z)
-                                   : 0.f;
+                        fz[f] = zv ? st_dplus(z1, cw[f][1], z2, zm1, c9z, c24z) : 0.f;
                         cw[f][0] = cw[f][1];
                         cw[f][1] = cw[f][2];
                         cw[f][2] = cw[f][3];
@@ -472,8 +531,9 @@ __global__ void k_cluster_reduce(const float *__restrict__ kpart, int nslots, si
 
 size_t cluster_smem_bytes(bool psv, const ClusterGeom &g, int nz) {
     const int nv = psv ? 2 : 1;
+    const size_t stage = g.stage ? (size_t)nv * (2 * g.cols_per + 3) * nz : 0;
     return ((size_t)(psv ? 7 : 4) * cluster_row_stride(g.cols_per) * (nz + 4) + (g.cols_per + 4) + g.nrec_cta +
-            (size_t)(g.nrec_cta + 1) * nv) *
+            (size_t)(g.nrec_cta + 1) * nv + stage) *
            4;
 }
 

@@ -95,6 +95,7 @@ struct TileCfg {
 // step and stencil coefficients), which the kernel reads from its parameters.
 struct ClusterGeom {
     int R, cols_per, G, qmax, nrec_cta;
+    int stage;  // adjoint: stage each checkpoint in shared memory before the kernel accumulation
     int nx, nz, nt;
     float dt, c9x, c24x, c9z, c24z;
 };

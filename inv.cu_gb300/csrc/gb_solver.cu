@@ -173,6 +173,7 @@ int Solver::init(const Config &cfg, int nx_, int nz_, float xmax_, float zmax_) 
     if (cfg.has("ckpt_precision")) opt_ckpt = cfg.iv("ckpt_precision");
     if (cfg.has("tile")) opt_tile = cfg.iv("tile");
     if (cfg.has("tma")) opt_tma = cfg.iv("tma") != 0;
+    if (cfg.has("cluster_stage")) opt_stage = cfg.iv("cluster_stage") != 0;
     if (cfg.has("cluster")) opt_cluster = std::max(0, std::min(16, cfg.iv("cluster")));
     nx = nx_;
     nz = nz_;
@@ -873,7 +874,7 @@ bool Solver::cluster_geometry(bool wave_psv, int n, ClusterGeom *out) const {
     const int rlo = opt_cluster >= 2 ? opt_cluster : 1, rhi = opt_cluster >= 2 ? opt_cluster : 16;
     for (int R = rlo; R <= rhi; R++) {
         for (int qm : {4, 8, 12, 16, 24}) {
-            ClusterGeom g;
+            ClusterGeom g{};
             g.R = R;
             g.qmax = qm;
             g.cols_per = ((nx + R - 1) / R + qm - 1) / qm * qm;
@@ -919,7 +920,7 @@ bool Solver::cluster_ok(const int *shots, int n, bool snapshot) const {
     if (!opt_cluster || snapshot || !rec_distinct || opt_ckpt != CKPT_F32 || nrec >= 0xffff) return false;
     for (int b = 0; b < n; b++)
         if (shots[b] < 0) return false;
-    ClusterGeom g;
+    ClusterGeom g{};
     if (sh && !cluster_geometry(false, n, &g)) return false;
     if (psv && !cluster_geometry(true, n, &g)) return false;
     return true;
@@ -943,10 +944,19 @@ int Solver::run_cluster_pass(int kind, int n) {
     for (int w = 0; w < 2; w++) {
         const bool wp = w == 1;
         if (wp ? !psv : !sh) continue;
-        ClusterGeom g;
+        ClusterGeom g{};
         if (!cluster_geometry(wp, n, &g)) {
             set_error("cluster pass: no geometry fits");
             return GB_ERR_STATE;
+        }
+        // adjoint: stage each checkpoint in shared memory when that fits
+        // without losing resident clusters
+        if (adjp && opt_stage && opt_ckpt == CKPT_F32) {
+            ClusterGeom gs = g;
+            gs.stage = 1;
+            if (cluster_smem_bytes(wp, gs, nz) <= 227 * 1024 - 64 &&
+                cluster_occupancy(wp, gs, nz) >= cluster_occupancy(wp, g, nz))
+                g.stage = 1;
         }
         // the same values as every slot's (fill_slots)
         g.nx = nx;

@@ -77,6 +77,31 @@ def test_cluster_sizes_match_step_kernels(gpu, orc, wave, nx, size):
         assert cases.rel(k_c[n], k_t[n]) < 1e-6, n
 
 
+@pytest.mark.parametrize("wave,nx,nz", [("sh", 681, 141), ("psv", 150, 110)])
+def test_cluster_checkpoint_staging_identical(gpu, orc, wave, nx, nz):
+    """The adjoint's kernel accumulation gives the same bits whether each
+    checkpoint is staged in shared memory or read from HBM."""
+    case = cases.make_case(wave=wave, nx=nx, nz=nz, nt=200, nsrc=2, nrec=min(nx - 4, 60), sfe=10, seed=nz)
+    rng = np.random.default_rng(3)
+    ad = [{c: (rng.standard_normal((case["nrec"], 200)) * 1e-3).astype(np.float32) for c in "xyz"}
+          for _ in range(2)]
+    out = []
+    for stage in (1, 0):
+        cfg, sol = cases.gpu_solver(gpu, case)
+        sol.set_option("cluster_stage", stage)
+        shots = [0, 1]
+        sol.run_forward_batch(shots)
+        for b in shots:
+            for c in comps(wave):
+                sol.set_adstf(c, ad[b][c], slot=b)
+        sol.initKernels()
+        sol.run_adjoint_batch(shots)
+        assert sol.stats().tile_tz < 0
+        out.append(sol.kernels())
+    for n in names(wave):
+        np.testing.assert_array_equal(out[0][n], out[1][n])
+
+
 def test_cluster_adjoint_matches_oracle(gpu, orc):
     case = cases.make_case(wave="psv", nx=120, nz=96, nt=400, nsrc=2, nrec=40, sfe=10, seed=11)
     pb = cases.oracle_problem(orc, case)
