@@ -535,6 +535,8 @@ def run_c4(args):
         reqs.append(dict(psv=psv, nx=nx, nz=nz, dx=10.0, dt=8e-4, nt=nt, lam=lam, mu=mu, rho=rho, src=src,
                          rec=rec))
     srv = pkg.Server(sfe=10, ckpt=2)
+    if args.server_tile:
+        srv.set_option("tile", args.server_tile)
     for q, r in enumerate(reqs):
         srv.submit(arrival=float(arrivals[q]), **r)
     srv.run()
@@ -542,6 +544,10 @@ def run_c4(args):
     # the same requests, one at a time (first `seq` of them)
     seq = min(nreq, args.sequential)
     one = pkg.Server(sfe=10, ckpt=2, max_slots=1)
+    # one request at a time: the 2-D tile kernel (configuration 3) is the
+    # faster choice for a lone grid of these sizes, the marching strips only
+    # pay off with many requests in flight
+    one.set_option("tile", 3)
     for r in reqs[:seq]:
         one.submit(arrival=0.0, **r)
     one.run()
@@ -698,6 +704,8 @@ def main():
     ap.add_argument("--requests", type=int, default=512, help="c4 request count")
     ap.add_argument("--rate", type=float, default=20.0, help="c4 Poisson arrival rate (requests/s)")
     ap.add_argument("--sequential", type=int, default=64, help="c4 requests also solved one at a time")
+    ap.add_argument("--server-tile", type=int, default=0,
+                    help="c4 step kernel configuration (0: the engine's default)")
     ap.add_argument("--profile-case", default="", help="run one small case for an ncu capture")
     ap.add_argument("--tile", type=int, default=3, help="kernel configuration for --profile-case")
     ap.add_argument("--cluster", type=int, default=0,

@@ -262,6 +262,9 @@ typedef struct {
     long long rounds, launches, cell_updates;
 } gb_server_stats;
 gb_server *gb_server_create(int sfe, int ckpt_precision, double hbm_budget_gb, int max_slots);
+/* Options, set before gb_server_run: "tile" (step kernel configuration 1..20,
+ * as gb_solver_set_option; default 11, marching strips of 152 rows). */
+int gb_server_set_option(gb_server *srv, const char *key, double value);
 /* Queues a request; returns its id (>= 0) or -1. */
 long long gb_server_submit(gb_server *srv, const gb_request_desc *req);
 /* Replays every queued request against the wall clock until all are done. */

@@ -134,6 +134,7 @@ def _declare(lib):
         "gb_device_select": (ctypes.c_int, [ctypes.c_int]),
         "gb_solver_timer": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
         "gb_server_create": (_vp, [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int]),
+        "gb_server_set_option": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_double]),
         "gb_server_submit": (ctypes.c_longlong, [_vp, ctypes.POINTER(RequestDesc)]),
         "gb_server_run": (ctypes.c_int, [_vp]),
         "gb_server_result": (ctypes.c_int, [_vp, ctypes.c_longlong, _fp, _fp, _fp, ctypes.POINTER(ctypes.c_double),
@@ -539,6 +540,10 @@ class Server:
         if not self._h:
             raise GbError(last_error())
         self._keep = {}
+
+    def set_option(self, key, value):
+        """Engine option set before run(): "tile" (step kernel configuration 1..20)."""
+        check(lib().gb_server_set_option(self._h, key.encode(), float(value)))
 
     def submit(self, *, psv, nx, nz, dx, dt, nt, lam, mu, rho, src, rec, obs=None, arrival=0.0, abs_width=20,
                abs_alpha=0.015, abs_edges=(1, 1, 1, 0), inv=(1, 1, 1), dz=None) -> int:

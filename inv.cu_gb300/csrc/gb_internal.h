@@ -84,6 +84,8 @@ struct KernelGroup {
 struct TileCfg {
     int tz, tx, threads;
 };
+// The step kernel configurations 1..20 (1-5: 2-D tiles, 6-20: marching strips).
+TileCfg tile_config(int id);
 
 // Cluster-resident solver geometry: R CTAs per shot (cluster), cols_per grid
 // columns per CTA (a multiple of qmax; the last CTA holds the remaining grid

@@ -24,6 +24,7 @@
 #include <cstring>
 #include <deque>
 #include <map>
+#include <string>
 #include <thread>
 #include <vector>
 
@@ -43,8 +44,9 @@ cudaError_t launch_waveform_refs(const void *refs, const float *tw, int ntr, int
 
 namespace {
 
-constexpr int kServerTile = 3;  // 2-D tiles 32 x 16: good across request sizes
-const TileCfg kSrvTile = {32, 16, 0};
+// Default step kernel configuration: marching strips of 152 rows, chunks of
+// 64 columns (option "tile" selects any of the solver's 1..20).
+constexpr int kServerTile = 11;
 
 struct Req {
     long long id = 0;
@@ -74,6 +76,7 @@ size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
 struct Server {
     int sfe = 10, prec = CKPT_F32, max_slots = 64;
+    TileCfg tile = {0, 0, 0};  // step kernel configuration (set at creation)
     double budget = 0;
     size_t used = 0;
     cudaStream_t st = nullptr;
@@ -121,9 +124,10 @@ struct gb_server {
 
 namespace {
 
-std::vector<int> csr_for(int nx, int nz, const std::vector<int> &ii, const std::vector<int> &jj, bool inj) {
-    // same packing as the solver's tables (tile 32 x 16)
-    const int tz = kSrvTile.tz, tx = kSrvTile.tx;
+std::vector<int> csr_for(TileCfg tc, int nx, int nz, const std::vector<int> &ii, const std::vector<int> &jj,
+                         bool inj) {
+    // same packing as the solver's tables
+    const int tz = tc.tz, tx = tc.tx;
     const int tiles_z = (nz + tz - 1) / tz, tiles_x = (nx + tx - 1) / tx, ntiles = tiles_z * tiles_x;
     const int vz = tz + 3;
     std::map<int, std::map<int, std::vector<int>>> per;
@@ -256,9 +260,9 @@ int admit(Server &S, Req &r) {
         ri[q] = calc_idx(d.rec[2 * q], xmax, d.nx);
         rj[q] = calc_idx(d.rec[2 * q + 1], zmax, d.nz);
     }
-    const std::vector<int> c1 = csr_for(d.nx, d.nz, si, sj, true);
-    const std::vector<int> c2 = csr_for(d.nx, d.nz, ri, rj, true);
-    const std::vector<int> c3 = csr_for(d.nx, d.nz, ri, rj, false);
+    const std::vector<int> c1 = csr_for(S.tile, d.nx, d.nz, si, sj, true);
+    const std::vector<int> c2 = csr_for(S.tile, d.nx, d.nz, ri, rj, true);
+    const std::vector<int> c3 = csr_for(S.tile, d.nx, d.nz, ri, rj, false);
     GB_CUDA_TRY(cudaMallocAsync((void **)&r.csr_src, (c1.size() + c2.size() + c3.size()) * 4, S.st));
     r.csr_rin = r.csr_src + c1.size();
     r.csr_rec = r.csr_rin + c2.size();
@@ -305,8 +309,8 @@ void fill_slot(const Server &S, const Req &r, Slot &s) {
     s.nx = d.nx;
     s.nz = d.nz;
     s.nt = d.nt;
-    s.tiles_z = (d.nz + kSrvTile.tz - 1) / kSrvTile.tz;
-    s.tiles_x = (d.nx + kSrvTile.tx - 1) / kSrvTile.tx;
+    s.tiles_z = (d.nz + S.tile.tz - 1) / S.tile.tz;
+    s.tiles_x = (d.nx + S.tile.tx - 1) / S.tile.tx;
     s.active = 1;
     s.it_base = r.it;
     s.par0 = r.it & 1;
@@ -430,7 +434,7 @@ int round_once(Server &S, std::vector<Req *> &act) {
                 GB_CUDA_TRY(launch_ckpt_store(tab, cnt, (int)max_n_fwd[w], k, 1, w, S.st));
                 S.launches += q16 ? 2 : 1;
             }
-            GB_CUDA_TRY(launch_step(w, kSrvTile, tab, cnt, max_tiles[w], k, false, S.st));
+            GB_CUDA_TRY(launch_step(w, S.tile, tab, cnt, max_tiles[w], k, false, S.st));
             S.launches++;
             if (k == S.sfe - 1 && cnt > nadj) {
                 if (q16) GB_CUDA_TRY(launch_ckpt_amax(tab, cnt, (int)max_n_fwd[w], k, 0, w, S.st));
@@ -470,7 +474,24 @@ gb_server *gb_server_create(int sfe, int ckpt_precision, double hbm_budget_gb, i
         return nullptr;
     }
     S.budget = hbm_budget_gb > 0 ? hbm_budget_gb * 1e9 : 0.8 * (double)freeb;
+    S.tile = tile_config(kServerTile);
     return h;
+}
+
+int gb_server_set_option(gb_server *h, const char *key, double value) {
+    if (!h || !key) return GB_ERR_ARG;
+    const std::string k = key;
+    if (k == "tile") {
+        const int t = (int)value;
+        if (t < 1 || t > 20) {
+            set_error("gb_server_set_option: tile must be 1..20");
+            return GB_ERR_ARG;
+        }
+        h->s.tile = tile_config(t);
+        return GB_OK;
+    }
+    set_error("gb_server_set_option: unknown option " + k);
+    return GB_ERR_ARG;
 }
 
 long long gb_server_submit(gb_server *h, const gb_request_desc *d) {

@@ -35,6 +35,8 @@ static const TileCfg kTiles[] = {
 };
 static const int kNumTiles = 20;
 
+TileCfg tile_config(int id) { return kTiles[id >= 1 && id <= kNumTiles ? id : 3]; }
+
 // ---------------------------------------------------------------- tables
 // Packs a point set into the tile CSR the step kernel reads. For injection
 // (inj = true) a point is listed for every tile whose velocity region (tile
