@@ -14,7 +14,8 @@
 //   phase B  velocity gradients and stress update
 //   barrier  (all stresses written before the next phase A reads them)
 // plus, in the adjoint, the kernel accumulation every sfe steps (one more
-// barrier). A thread that updates one of the CTA's edge columns also writes
+// barrier; its checkpoint is staged in shared memory during phase B when the
+// CTA has room). A thread that updates one of the CTA's edge columns also writes
 // the new value into the neighbouring CTA's ghost column (st.shared::cluster,
 // made visible by the cluster barrier's release/acquire), so the stencils
 // only ever read the CTA's own shared memory. The x-differences walk the
@@ -27,8 +28,6 @@
 // contribution in a per-shot buffer that is added to the kernels after the
 // pass, in shot order.
 #include <cooperative_groups.h>
-#include <cuda_bf16.h>
-#include <cuda_fp16.h>
 
 #include <algorithm>
 
@@ -72,13 +71,6 @@ __device__ __forceinline__ void cp_async4_zf(float *dst, const float *src, bool 
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
                  "l"(src), "r"(pred ? 4 : 0)
                  : "memory");
-}
-
-__device__ __forceinline__ float ck_get(const Slot &S, int isfe, int q, size_t k, size_t n, float inv) {
-    const size_t off = ((size_t)isfe * S.nf + q) * n + k;
-    if (S.ckpt_prec == CKPT_F32) return __ldg(static_cast<const float *>(S.ckpt) + off);
-    if (S.ckpt_prec == CKPT_BF16) return __bfloat162float(static_cast<const __nv_bfloat16 *>(S.ckpt)[off]) * inv;
-    return __half2float(static_cast<const __half *>(S.ckpt)[off]) * inv;
 }
 
 // Shared-memory field order. P-SV: vx vz ux uz sxx szz sxz; SH: vy uy sxy szy.
@@ -421,11 +413,13 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
         }
         cl.sync();
         // ---- adjoint: kernel accumulation every sfe steps (solver/fdm.h:583-606)
-        // FP32 checkpoints (the only precision this path takes): the
-        // x-differences walk the thread's columns with a window over the
-        // checkpointed displacement, so each column adds one checkpoint load
-        // per field; rows and columns are clamped to the grid, and a cell's
-        // differences are masked where the reference skips them.
+        // FP32 checkpoints (the only precision this path takes), copied into
+        // shared memory at the start of phase B when g.stage, else read from
+        // HBM: the x-differences walk the thread's columns with a window over
+        // the checkpointed displacement, so each column adds one load per
+        // field; rows and columns are clamped to the grid (HBM) or zero-filled
+        // (staged), and a cell's differences are masked where the reference
+        // skips them. The per-shot kernel buffer takes the `-=`.
         if (ADJ && S.ckpt && S.sfe > 0 && it % S.sfe == 0 && it / S.sfe < S.nsfe) {
             const int isfe_a = it / S.sfe;
             const float ndt = (float)S.sfe * dt;
