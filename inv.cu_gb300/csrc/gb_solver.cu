@@ -800,6 +800,7 @@ int Solver::run_pass(int kind, int n, bool snapshot, int snap_isrc) {
     }
     GB_CUDA_TRY(cudaEventRecord(ev_pass0, st));
     GB_CUDA_TRY(launch_reciprocal(rinv, rho, ncell(), st));
+    stats.launches += 1;
     if (opt_graphs && !snapshot) {
         auto key = std::make_pair(kind, n);
         auto g = graphs.find(key);
@@ -933,6 +934,7 @@ int Solver::run_cluster_pass(int kind, int n) {
     const size_t nc = ncell();
     GB_CUDA_TRY(cudaEventRecord(ev_pass0, st));
     GB_CUDA_TRY(launch_reciprocal(rinv, rho, nc, st));
+    stats.launches += 1;
     const bool adjp = kind == PASS_ADJ;
     if (adjp) {
         if (kpart_slots < (size_t)n) {
