@@ -1,0 +1,106 @@
+"""Parity at the benchmark configurations' full sizes.
+
+The oracle finishes a full P-SV shot of the 200x200 configuration in
+seconds, so that one is compared directly. At the larger sizes the checks
+are properties that do not depend on the size: the cluster-resident pass
+and the per-step kernels, and the marching kernel's two load paths, compute
+every cell with the same operations, so their seismograms must agree bit for
+bit over the whole time loop."""
+import numpy as np
+import pytest
+
+from tests import cases
+
+pytestmark = pytest.mark.gpu
+
+
+def surface_receivers(case, h):
+    """One receiver per column, two cells deep (distinct cells)."""
+    case["rec"] = [[i * h, 2 * h] for i in range(case["nx"])]
+    case["nrec"] = case["nx"]
+    return case
+
+
+def test_c1_full_psv_forward_matches_oracle(gpu, orc):
+    """P-SV 200x200 at 10 m, dt 1 ms, 2000 steps, receivers in every column,
+    through the cluster pass. FP32 round-off of the reference's scheme grows
+    over this run (the oracle's own FP32 and FP64 builds end ~1e-3 apart), so:
+    the first 1000 steps match the FP32 oracle to 1e-5, and over the whole
+    loop the GPU is as close to the FP64 solution as FP32 arithmetic in the
+    reference's order is (within a factor 2)."""
+    h = 10.0
+    case = surface_receivers(cases.make_case(wave="psv", nx=200, nz=200, nt=2000, nsrc=4, dx=h, dt=1e-3, f0=10.0,
+                                             abs_width=20, sfe=10, seed=1), h)
+    cfg, sol = cases.gpu_solver(gpu, case)
+    sol.run_forward_batch([0, 1, 2, 3])
+    assert sol.stats().tile_tz < 0, "the cluster path did not run"
+    pb = cases.oracle_problem(orc, case)
+    o32 = orc.forward(pb, 2, adj=True)
+    o64 = orc.forward(pb, 2, adj=True, precision="f64")
+    for q, c in ((0, "x"), (2, "z")):
+        g = sol.out(c, slot=2)
+        assert cases.rel(g[:, :1000], o32[q][:, :1000]) < 1e-5, c
+        assert cases.rel(g, o64[q]) <= 2.0 * cases.rel(o32[q], o64[q]), c
+
+
+def test_c2_full_cluster_equals_step_kernels(gpu, orc):
+    """SH 681x141 at 12.5 m, 4000 steps, 16 shots, 681 receivers, FP32
+    checkpoints every 10 steps: forward seismograms of the cluster pass and
+    of the per-step kernels are identical and match the oracle; the kernels
+    differ only by the order the shots are summed."""
+    h = 12.5
+    case = surface_receivers(cases.make_case(wave="sh", nx=681, nz=141, nt=4000, nsrc=16, dx=h, dt=1e-3, f0=8.0,
+                                             abs_width=20, sfe=10, seed=2), h)
+    rng = np.random.default_rng(4)
+    ad = [(rng.standard_normal((681, 4000)) * 1e-3).astype(np.float32) for _ in range(16)]
+    shots = list(range(16))
+    res = []
+    for cluster in (1, 0):
+        cfg, sol = cases.gpu_solver(gpu, case)
+        sol.set_option("cluster", cluster)
+        sol.run_forward_batch(shots)
+        tr = [sol.out("y", slot=b) for b in shots]
+        assert (sol.stats().tile_tz < 0) == (cluster == 1)
+        for b in shots:
+            sol.set_adstf("y", ad[b], slot=b)
+        sol.initKernels()
+        sol.run_adjoint_batch(shots)
+        res.append((tr, sol.kernels()))
+        sol.close()
+    for b in shots:
+        np.testing.assert_array_equal(res[0][0][b], res[1][0][b])
+    for n in ("k_mu", "k_rho"):
+        assert cases.rel(res[0][1][n], res[1][1][n]) < 1e-6, n
+    # and the full 4000-step seismogram of one shot against the oracle (this
+    # SH configuration is well conditioned: FP32 and FP64 oracles agree to 2e-6)
+    o = orc.forward(cases.oracle_problem(orc, case), 0, adj=True)
+    assert cases.rel(res[0][0][0], o[1]) < 1e-5
+
+
+def test_c5_grid_bulk_loads_equal_cp_async(gpu, orc):
+    """P-SV 4096x1024 (the full-inversion grid), 2 shots, 40 steps: the
+    marching kernel with bulk tensor loads and with per-row cp.async."""
+    case = cases.make_case(wave="psv", nx=4096, nz=1024, nt=40, nsrc=2, nrec=256, dx=5.0, dt=4e-4, f0=12.0,
+                           abs_width=20, sfe=10, seed=5)
+    rng = np.random.default_rng(6)
+    ad = {c: (rng.standard_normal((256, 40)) * 1e-3).astype(np.float32) for c in "xz"}
+    res = []
+    for tma in (1, 0):
+        cfg, sol = cases.gpu_solver(gpu, case)
+        sol.set_option("cluster", 0)
+        sol.set_option("tile", 19)
+        sol.set_option("tma", tma)
+        sol.run_forward_batch([0, 1])
+        assert sol.stats().march_bulk == tma
+        tr = {c: sol.out(c, slot=1) for c in "xz"}
+        for b in (0, 1):
+            for c in "xz":
+                sol.set_adstf(c, ad[c], slot=b)
+        sol.initKernels()
+        sol.run_adjoint_batch([0, 1])
+        res.append((tr, sol.kernels()))
+        sol.close()
+    for c in "xz":
+        np.testing.assert_array_equal(res[0][0][c], res[1][0][c])
+    for n in ("k_lambda", "k_mu", "k_rho"):
+        np.testing.assert_array_equal(res[0][1][n], res[1][1][n])
