@@ -305,6 +305,10 @@ int gb_solver_set_option(gb_solver *s, const char *key, double value) {
             v.tuned = false;
         }
         v.invalidate_graphs();
+    } else if (k == "cluster_qm") {
+        const int q = (int)value;
+        if (q != 0 && q != 4 && q != 8 && q != 10 && q != 12 && q != 16 && q != 20 && q != 24) return GB_ERR_ARG;
+        v.opt_cluster_qm = q;
     } else if (k == "cluster_stage") {
         v.opt_stage = value != 0;
     } else if (k == "tma") {

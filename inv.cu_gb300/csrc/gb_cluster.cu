@@ -42,8 +42,8 @@ namespace gb {
 // owned cell for SH, 3 for P-SV) plus about 56 (SH) or 64 (P-SV) registers of
 // per-thread state must fit in the 65536-register file of the SM.
 __host__ __device__ constexpr int cluster_threads_for(bool psv, int qm) {
-    return psv ? (qm <= 4 ? 800 : qm <= 8 ? 736 : qm <= 12 ? 608 : qm <= 16 ? 576 : 480)
-               : (qm <= 4 ? 1024 : qm <= 8 ? 896 : qm <= 12 ? 800 : qm <= 16 ? 736 : 608);
+    return psv ? (qm <= 4 ? 800 : qm <= 8 ? 736 : qm <= 10 ? 640 : qm <= 12 ? 608 : qm <= 16 ? 576 : qm <= 20 ? 512 : 480)
+               : (qm <= 4 ? 1024 : qm <= 10 ? 896 : qm <= 12 ? 800 : qm <= 16 ? 736 : qm <= 20 ? 640 : 608);
 }
 
 int cluster_max_threads(bool psv, int qm) { return cluster_threads_for(psv, qm); }
@@ -538,6 +538,8 @@ static void *cluster_kernel_q(int qm) {
     case 8: return (void *)k_cluster<PSV, ADJ, 8>;
     case 12: return (void *)k_cluster<PSV, ADJ, 12>;
     case 16: return (void *)k_cluster<PSV, ADJ, 16>;
+    case 10: return (void *)k_cluster<PSV, ADJ, 10>;
+    case 20: return (void *)k_cluster<PSV, ADJ, 20>;
     case 24: return (void *)k_cluster<PSV, ADJ, 24>;
     default: return nullptr;
     }

@@ -91,8 +91,8 @@ TileCfg tile_config(int id);
 // columns per CTA (a multiple of qmax; the last CTA holds the remaining grid
 // columns, at least 2), G groups of nz threads per CTA (blockDim = G * nz),
 // each thread owning qmax consecutive columns of one row (qmax in
-// {4, 8, 12, 16, 24}, G * qmax = cols_per); nrec_cta = most receivers in one
-// CTA's columns.
+// {4, 8, 10, 12, 16, 20, 24}, G * qmax = cols_per); nrec_cta = most receivers
+// in one CTA's columns.
 // The launch also carries the values common to all slots (grid, steps, time
 // step and stencil coefficients), which the kernel reads from its parameters.
 struct ClusterGeom {

@@ -175,6 +175,7 @@ int Solver::init(const Config &cfg, int nx_, int nz_, float xmax_, float zmax_) 
     if (cfg.has("ckpt_precision")) opt_ckpt = cfg.iv("ckpt_precision");
     if (cfg.has("tile")) opt_tile = cfg.iv("tile");
     if (cfg.has("tma")) opt_tma = cfg.iv("tma") != 0;
+    if (cfg.has("cluster_qm")) opt_cluster_qm = cfg.iv("cluster_qm");
     if (cfg.has("cluster_stage")) opt_stage = cfg.iv("cluster_stage") != 0;
     if (cfg.has("cluster")) opt_cluster = std::max(0, std::min(16, cfg.iv("cluster")));
     nx = nx_;
@@ -865,7 +866,7 @@ int Solver::run_pass(int kind, int n, bool snapshot, int snap_isrc) {
 // allowance) times the number of cluster rounds the batch needs.
 bool Solver::cluster_geometry(bool wave_psv, int n, ClusterGeom *out) const {
     if (nx < 2 || nz < 1) return false;
-    const long long key = ((long long)n * 32 + opt_cluster) * 2 + (wave_psv ? 1 : 0);
+    const long long key = (((long long)n * 32 + opt_cluster) * 32 + opt_cluster_qm) * 2 + (wave_psv ? 1 : 0);
     const auto hit = cluster_cache.find(key);
     if (hit != cluster_cache.end()) {
         if (hit->second.first) *out = hit->second.second;
@@ -876,7 +877,8 @@ bool Solver::cluster_geometry(bool wave_psv, int n, ClusterGeom *out) const {
     double best = -1;
     const int rlo = opt_cluster >= 2 ? opt_cluster : 1, rhi = opt_cluster >= 2 ? opt_cluster : 16;
     for (int R = rlo; R <= rhi; R++) {
-        for (int qm : {4, 8, 12, 16, 24}) {
+        for (int qm : {4, 8, 10, 12, 16, 20, 24}) {
+            if (opt_cluster_qm && qm != opt_cluster_qm) continue;
             ClusterGeom g{};
             g.R = R;
             g.qmax = qm;
