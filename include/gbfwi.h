@@ -141,7 +141,9 @@ int gb_solver_batch_capacity(gb_solver *s);
  * kernel loads grid columns with bulk tensor copies when nz % 4 == 0,
  * default; 0: per-thread cp.async), "cluster_stage" (1: a cluster adjoint
  * stages each checkpoint in shared memory before the kernel accumulation when
- * it fits, default; 0: reads it from HBM), "hbm_budget_gb". Options
+ * it fits, default; 0: reads it from HBM), "cluster_qm" (columns per
+ * thread of the cluster pass: 0 = chosen with the cluster size, or 4, 8, 10,
+ * 12, 16, 20, 24), "hbm_budget_gb". Options
  * change no forward result; "ckpt" changes kernels by the checkpoint
  * rounding and "cluster" by the order in which shots are summed. */
 int gb_solver_set_option(gb_solver *s, const char *key, double value);
