@@ -453,10 +453,26 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
             // staged checkpoint: displacement f at local column c + o (o >= -1), velocity f at c
             const float *su = ckst + (size_t)(cb + 1) * nz + j;
             const float *sv = ckst + ((size_t)NV * (cp + 3) + cb) * nz + j;
-            // four columns per iteration keep their kernel-buffer loads in flight together
-#pragma unroll 4
+            // The kernel buffer is read one column ahead of its update: the
+            // compiler cannot tell that columns q and q+1 are distinct
+            // addresses, so an in-place `-=` would wait for each store before
+            // the next load.
+            float nk[3] = {0.f, 0.f, 0.f};  // kernel buffer (lambda, mu, rho) at the next column
+            if (nq > 0) {
+                if (PSV) nk[0] = kl[0];
+                nk[1] = km[0];
+                nk[2] = kr[0];
+            }
+#pragma unroll 2
             for (int q = 0; q < QM; q++) {
                 if (q < nq) {
+                    const float ok[3] = {nk[0], nk[1], nk[2]};
+                    if (q + 1 < nq) {
+                        const size_t o1 = (size_t)(q + 1) * nz;
+                        if (PSV) nk[0] = kl[o1];
+                        nk[1] = km[o1];
+                        nk[2] = kr[o1];
+                    }
                     const bool gx = (xv_mask >> q) & 1;
                     float ux[NV], uzz[NV], fx[NV], fz[NV], vf[NV];
 #pragma unroll
@@ -492,12 +508,12 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
                     if (PSV) {
                         const float dvxdx = ux[0], dvxdz = uzz[0], dvzdx = ux[NV - 1], dvzdz = uzz[NV - 1];
                         const float fxdx = fx[0], fxdz = fz[0], fzdx = fx[NV - 1], fzdz = fz[NV - 1];
-                        kr[o] -= (vf[0] * v0[0] + vf[NV - 1] * v0[fs]) * ndt;
-                        km[o] -= (2.f * dvxdx * fxdx + 2.f * dvzdz * fzdz + (dvxdz + dvzdx) * (fzdx + fxdz)) * ndt;
-                        kl[o] -= ((dvxdx + dvzdz) * (fxdx + fzdz)) * ndt;
+                        kr[o] = ok[2] - (vf[0] * v0[0] + vf[NV - 1] * v0[fs]) * ndt;
+                        km[o] = ok[1] - (2.f * dvxdx * fxdx + 2.f * dvzdz * fzdz + (dvxdz + dvzdx) * (fzdx + fxdz)) * ndt;
+                        kl[o] = ok[0] - ((dvxdx + dvzdz) * (fxdx + fzdz)) * ndt;
                     } else {
-                        kr[o] -= vf[0] * v0[0] * ndt;
-                        km[o] -= (ux[0] * fx[0] + uzz[0] * fz[0]) * ndt;
+                        kr[o] = ok[2] - vf[0] * v0[0] * ndt;
+                        km[o] = ok[1] - (ux[0] * fx[0] + uzz[0] * fz[0]) * ndt;
                     }
                 }
             }
