@@ -134,13 +134,17 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
     float *s_sz = ring + kRing * W::N * T;               // [2][NZS][TP]
     float *s_vz = s_sz + 2 * NZS * TP;                   // [2][NV][TP]
 
-    const Slot &S = slots[blockIdx.y];
+    // Blocks run shot-minor (block b: shot b % nslots, tile b / nslots): the
+    // same strip of every shot runs close together, so the model columns,
+    // shared by the shots, are read from HBM once and from L2 after.
+    const unsigned blk = blockIdx.y * gridDim.x + blockIdx.x;
+    const Slot &S = slots[blk % gridDim.y];
     if (!S.active) return;
     const int it = S.it_base + kstep;
     if (it < 0 || it >= S.nt) return;
     const int par = (S.par0 + kstep) & 1;
     const int nx = S.nx, nz = S.nz, nt = S.nt;
-    const int tile = blockIdx.x;
+    const int tile = (int)(blk / gridDim.y);
     if (tile >= S.tiles_z * S.tiles_x) return;
     const int strip = tile % S.tiles_z, ck = tile / S.tiles_z;
     const int t = threadIdx.x;

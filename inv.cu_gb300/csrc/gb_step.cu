@@ -78,13 +78,17 @@ __global__ void __launch_bounds__(kThreads) k_step(const Slot *__restrict__ slot
     __shared__ float s_rho[NVR];  // reciprocal density
     __shared__ float s_inj[NV][kMaxInjTraces];
 
-    const Slot &S = slots[blockIdx.y];
+    // Blocks run shot-minor (block b: shot b % nslots, tile b / nslots): the
+    // same tile of every shot runs close together, so the model, shared by
+    // the shots, is read from HBM once and from L2 after.
+    const unsigned blk = blockIdx.y * gridDim.x + blockIdx.x;
+    const Slot &S = slots[blk % gridDim.y];
     if (!S.active) return;
     const int it = S.it_base + kstep;
     if (it < 0 || it >= S.nt) return;
     const int par = (S.par0 + kstep) & 1;
     const int nx = S.nx, nz = S.nz;
-    const int tile = blockIdx.x;
+    const int tile = (int)(blk / gridDim.y);
     if (tile >= S.tiles_z * S.tiles_x) return;
     const int tzi = tile % S.tiles_z, txi = tile / S.tiles_z;
     const int j0 = tzi * TZ, i0 = txi * TX;
