@@ -627,19 +627,32 @@ def run_profile_case(args):
         print("profile case", name, "cluster", args.cluster, "forward_ms %.3f adjoint_ms %.3f" % (st.forward_ms,
                                                                                             st.adjoint_ms))
         return
-    if name == "psv-2048x1024x2":
-        case = cases.make_case(wave="psv", nx=2048, nz=1024, nt=12, nsrc=2, nrec=256, seed=1, abs_width=20)
-    elif name == "sh-681x141x16":
-        case = cases.make_case(wave="sh", nx=681, nz=141, nt=12, nsrc=16, nrec=256, seed=1, abs_width=20)
-    else:
+    # "<psv|sh>-<nx>x<nz>x<shots>": a 12-step forward batch (the launches an
+    # ncu capture selects), then three more timed with the solver's CUDA
+    # events: time per step and algorithmic bandwidth (68 / 40 B per cell)
+    try:
+        wave, dims = name.split("-")
+        nx, nz, nshot = (int(v) for v in dims.split("x"))
+        assert wave in ("psv", "sh")
+    except (ValueError, AssertionError):
         raise SystemExit("unknown profile case " + name)
+    case = cases.make_case(wave=wave, nx=nx, nz=nz, nt=12, nsrc=nshot, nrec=min(nx - 4, 256), seed=1, abs_width=20)
     case["values"]["mode"] = 3
     cfg, sol = cases.gpu_solver(pkg, case)
     sol.set_option("tile", args.tile)
     sol.set_option("graphs", 0)
     sol.set_option("cluster", args.cluster)
-    sol.run_forward_batch(list(range(case["nsrc"])))
-    print("profile case", name, "tile", args.tile, "cluster", args.cluster, "done")
+    sol.set_option("tma", args.tma)
+    shots = list(range(nshot))
+    sol.run_forward_batch(shots)
+    sol.stats(reset=True)
+    for _ in range(3):
+        sol.run_forward_batch(shots)
+    st = sol.stats()
+    us = 1e3 * st.step_ms / max(st.step_launches, 1)
+    gbs = (68.0 if wave == "psv" else 40.0) * nx * nz * nshot / (us * 1e-6) / 1e9
+    print("profile case %s tile %d cluster %d: %.2f us per step, %.1f GB/s algorithmic, bulk loads %d" %
+          (name, args.tile, args.cluster, us, gbs, st.march_bulk))
 
 
 def run_reference(args, ws, rank):
@@ -708,6 +721,7 @@ def main():
                     help="c4 step kernel configuration (0: the engine's default)")
     ap.add_argument("--profile-case", default="", help="run one small case for an ncu capture")
     ap.add_argument("--tile", type=int, default=3, help="kernel configuration for --profile-case")
+    ap.add_argument("--tma", type=int, default=1, help="--profile-case: marching kernel bulk loads (1) or cp.async (0)")
     ap.add_argument("--cluster", type=int, default=0,
                     help="--profile-case: 0 per-step kernels, 1 cluster-resident (automatic size), 2..16 that size")
     args = ap.parse_args()
