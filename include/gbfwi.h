@@ -141,7 +141,9 @@ int gb_solver_batch_capacity(gb_solver *s);
  * kernel loads grid columns with bulk tensor copies when nz % 4 == 0,
  * default; 0: per-thread cp.async), "cluster_stage" (1: a cluster adjoint
  * stages each checkpoint in shared memory before the kernel accumulation when
- * it fits, default; 0: reads it from HBM), "cluster_qm" (columns per
+ * it fits; 0: reads it from HBM, default), "cluster_kacc" (1: a cluster
+ * adjoint keeps each shot's kernels in shared memory for the whole pass when
+ * they fit, default; 0: adds into an HBM buffer), "cluster_qm" (columns per
  * thread of the cluster pass: 0 = chosen with the cluster size, or 4, 8, 10,
  * 12, 16, 20, 24), "hbm_budget_gb". Options
  * change no forward result; "ckpt" changes kernels by the checkpoint
@@ -153,7 +155,9 @@ int gb_solver_set_option(gb_solver *s, const char *key, double value);
  * consecutive launches; launches: kernels (or graph kernel nodes) enqueued.
  * tile_tz, tile_tx: kernel configuration of the last pass (tile_tz = -R for
  * a cluster-resident pass of R-CTA clusters); march_bulk: 1 when the last
- * marching-kernel pass loaded its columns with bulk tensor copies. */
+ * marching-kernel pass loaded its columns with bulk tensor copies;
+ * cluster_adj: shared-memory use of the last cluster-resident adjoint pass,
+ * bit 0 checkpoints staged, bit 1 kernels accumulated there. */
 typedef struct {
     double forward_ms, adjoint_ms, misfit_ms, filter_ms;
     double step_ms;
@@ -162,6 +166,7 @@ typedef struct {
     long long cell_updates;
     int tile_tz, tile_tx, batch_capacity;
     int march_bulk;
+    int cluster_adj;
 } gb_stats;
 int gb_solver_stats(gb_solver *s, gb_stats *out, int reset);
 

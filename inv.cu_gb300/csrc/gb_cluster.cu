@@ -14,8 +14,8 @@
 //   phase B  velocity gradients and stress update
 //   barrier  (all stresses written before the next phase A reads them)
 // plus, in the adjoint, the kernel accumulation every sfe steps (one more
-// barrier; its checkpoint is staged in shared memory during phase B when the
-// CTA has room). A thread that updates one of the CTA's edge columns also writes
+// barrier; the shot's kernels stay in shared memory for the whole pass when
+// the CTA has room, and the checkpoint can be staged there during phase B). A thread that updates one of the CTA's edge columns also writes
 // the new value into the neighbouring CTA's ghost column (st.shared::cluster,
 // made visible by the cluster barrier's release/acquire), so the stencils
 // only ever read the CTA's own shared memory. The x-differences walk the
@@ -25,8 +25,9 @@
 // Every cell is computed with the operations, in the order, of the fused
 // step kernels (gb_stencil.h): forward traces and checkpoints are
 // bit-identical to theirs. The adjoint accumulates each shot's kernel
-// contribution in a per-shot buffer that is added to the kernels after the
-// pass, in shot order.
+// contribution in a per-shot buffer (directly, or from the shared-memory
+// accumulators at the end of the pass) that is added to the kernels after
+// the pass, in shot order.
 #include <cooperative_groups.h>
 
 #include <algorithm>
@@ -123,6 +124,10 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
     // NV displacement fields over columns -1 .. cp+1 and NV velocity fields
     // over columns 0 .. cp-1, stored by columns ([field][column][row])
     float *ckst = sbuf + NV;
+    // adjoint with g.kacc: the shot's kernels of the CTA's columns (P-SV lambda,
+    // mu, rho; SH mu, rho), [kernel][column][row], zero at the start of the pass
+    constexpr int NKA = PSV ? 3 : 2;
+    float *kacc = ckst + (g.stage ? (size_t)NV * (2 * cp + 3) * nz : 0);
     __shared__ int s_count;
     int *map = reinterpret_cast<int *>(sm);
     for (int e = t; e < cp * nz; e += blockDim.x) map[e] = -1;
@@ -155,6 +160,8 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
     const unsigned spmask = rmask | (srcq >= 0 ? 1u << srcq : 0u);
     __syncthreads();
     for (int e = t; e < NF * fs; e += blockDim.x) sm[e] = 0.f;
+    if (ADJ && g.kacc)
+        for (int e = t; e < NKA * cp * nz; e += blockDim.x) kacc[e] = 0.f;
     for (int c = t - 2; c < cp + 2; c += blockDim.x) s_ax[c + 2] = __ldg(S.ax + min(max(x0 + c, 0), nx - 1));
 
     // model of the owned cells
@@ -419,7 +426,8 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
         // the checkpointed displacement, so each column adds one load per
         // field; rows and columns are clamped to the grid (HBM) or zero-filled
         // (staged), and a cell's differences are masked where the reference
-        // skips them. The per-shot kernel buffer takes the `-=`.
+        // skips them. The shared accumulators (g.kacc) or the per-shot kernel
+        // buffer take the `-=`.
         if (ADJ && S.ckpt && S.sfe > 0 && it % S.sfe == 0 && it / S.sfe < S.nsfe) {
             const int isfe_a = it / S.sfe;
             const float ndt = (float)S.sfe * dt;
@@ -449,6 +457,11 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
             float *kl = kpart + ((size_t)slot * 3 + 0) * ncell + kc;
             float *km = kpart + ((size_t)slot * 3 + 1) * ncell + kc;
             float *kr = kpart + ((size_t)slot * 3 + 2) * ncell + kc;
+            // or the shared accumulators of the thread's first cell
+            const bool kin = g.kacc != 0;
+            float *al = kacc + (size_t)cb * nz + j;
+            float *am = al + (PSV ? (size_t)cp * nz : 0);
+            float *ar = am + (size_t)cp * nz;
             const bool staged = g.stage != 0;  // staging copies waited for above
             // staged checkpoint: displacement f at local column c + o (o >= -1), velocity f at c
             const float *su = ckst + (size_t)(cb + 1) * nz + j;
@@ -458,7 +471,7 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
             // addresses, so an in-place `-=` would wait for each store before
             // the next load.
             float nk[3] = {0.f, 0.f, 0.f};  // kernel buffer (lambda, mu, rho) at the next column
-            if (nq > 0) {
+            if (nq > 0 && !kin) {
                 if (PSV) nk[0] = kl[0];
                 nk[1] = km[0];
                 nk[2] = kr[0];
@@ -466,8 +479,13 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
 #pragma unroll 2
             for (int q = 0; q < QM; q++) {
                 if (q < nq) {
-                    const float ok[3] = {nk[0], nk[1], nk[2]};
-                    if (q + 1 < nq) {
+                    const size_t o = (size_t)q * nz;
+                    float ok[3] = {nk[0], nk[1], nk[2]};
+                    if (kin) {
+                        ok[0] = PSV ? al[o] : 0.f;
+                        ok[1] = am[o];
+                        ok[2] = ar[o];
+                    } else if (q + 1 < nq) {
                         const size_t o1 = (size_t)(q + 1) * nz;
                         if (PSV) nk[0] = kl[o1];
                         nk[1] = km[o1];
@@ -504,21 +522,39 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
                         cw[f][2] = cw[f][3];
                     }
                     const float *v0 = P + FV * fs + q;
-                    const size_t o = (size_t)q * nz;
+                    float nl = 0.f, nm, nr;
                     if (PSV) {
                         const float dvxdx = ux[0], dvxdz = uzz[0], dvzdx = ux[NV - 1], dvzdz = uzz[NV - 1];
                         const float fxdx = fx[0], fxdz = fz[0], fzdx = fx[NV - 1], fzdz = fz[NV - 1];
-                        kr[o] = ok[2] - (vf[0] * v0[0] + vf[NV - 1] * v0[fs]) * ndt;
-                        km[o] = ok[1] - (2.f * dvxdx * fxdx + 2.f * dvzdz * fzdz + (dvxdz + dvzdx) * (fzdx + fxdz)) * ndt;
-                        kl[o] = ok[0] - ((dvxdx + dvzdz) * (fxdx + fzdz)) * ndt;
+                        nr = ok[2] - (vf[0] * v0[0] + vf[NV - 1] * v0[fs]) * ndt;
+                        nm = ok[1] - (2.f * dvxdx * fxdx + 2.f * dvzdz * fzdz + (dvxdz + dvzdx) * (fzdx + fxdz)) * ndt;
+                        nl = ok[0] - ((dvxdx + dvzdz) * (fxdx + fzdz)) * ndt;
                     } else {
-                        kr[o] = ok[2] - vf[0] * v0[0] * ndt;
-                        km[o] = ok[1] - (ux[0] * fx[0] + uzz[0] * fz[0]) * ndt;
+                        nr = ok[2] - vf[0] * v0[0] * ndt;
+                        nm = ok[1] - (ux[0] * fx[0] + uzz[0] * fz[0]) * ndt;
+                    }
+                    if (kin) {
+                        ar[o] = nr;
+                        am[o] = nm;
+                        if (PSV) al[o] = nl;
+                    } else {
+                        kr[o] = nr;
+                        km[o] = nm;
+                        if (PSV) kl[o] = nl;
                     }
                 }
             }
             cl.sync();
         }
+    }
+    // the shared accumulators (written by this thread only) go to the shot's buffer
+    if (ADJ && g.kacc) {
+        const size_t kc = (size_t)i0 * nz + j;
+#pragma unroll 1
+        for (int q = 0; q < nq; q++)
+#pragma unroll
+            for (int k = 0; k < NKA; k++)
+                kpart[((size_t)slot * 3 + (PSV ? k : k + 1)) * ncell + kc + (size_t)q * nz] = kacc[((size_t)k * cp + cb + q) * nz + j];
     }
 }
 
@@ -542,8 +578,9 @@ __global__ void k_cluster_reduce(const float *__restrict__ kpart, int nslots, si
 size_t cluster_smem_bytes(bool psv, const ClusterGeom &g, int nz) {
     const int nv = psv ? 2 : 1;
     const size_t stage = g.stage ? (size_t)nv * (2 * g.cols_per + 3) * nz : 0;
+    const size_t kacc = g.kacc ? (size_t)(psv ? 3 : 2) * g.cols_per * nz : 0;
     return ((size_t)(psv ? 7 : 4) * cluster_row_stride(g.cols_per) * (nz + 4) + (g.cols_per + 4) + g.nrec_cta +
-            (size_t)(g.nrec_cta + 1) * nv + stage) *
+            (size_t)(g.nrec_cta + 1) * nv + stage + kacc) *
            4;
 }
 

@@ -98,6 +98,7 @@ TileCfg tile_config(int id);
 struct ClusterGeom {
     int R, cols_per, G, qmax, nrec_cta;
     int stage;  // adjoint: stage each checkpoint in shared memory before the kernel accumulation
+    int kacc;   // adjoint: accumulate the shot's kernels in shared memory, stored once after the pass
     int nx, nz, nt;
     float dt, c9x, c24x, c9z, c24z;
 };

@@ -177,6 +177,7 @@ int Solver::init(const Config &cfg, int nx_, int nz_, float xmax_, float zmax_) 
     if (cfg.has("tma")) opt_tma = cfg.iv("tma") != 0;
     if (cfg.has("cluster_qm")) opt_cluster_qm = cfg.iv("cluster_qm");
     if (cfg.has("cluster_stage")) opt_stage = cfg.iv("cluster_stage") != 0;
+    if (cfg.has("cluster_kacc")) opt_kacc = cfg.iv("cluster_kacc") != 0;
     if (cfg.has("cluster")) opt_cluster = std::max(0, std::min(16, cfg.iv("cluster")));
     nx = nx_;
     nz = nz_;
@@ -955,14 +956,25 @@ int Solver::run_cluster_pass(int kind, int n) {
             set_error("cluster pass: no geometry fits");
             return GB_ERR_STATE;
         }
-        // adjoint: stage each checkpoint in shared memory when that fits
-        // without losing resident clusters
+        // adjoint: keep the shot's kernels in shared memory for the whole
+        // pass, and stage each checkpoint there, when that fits without
+        // adding cluster rounds for this batch (the accumulators first)
+        const int occ0 = adjp ? std::max(1, cluster_occupancy(wp, g, nz)) : 1;
+        const int rounds = (n + occ0 - 1) / occ0;
+        auto fits = [&](const ClusterGeom &h) {
+            if (cluster_smem_bytes(wp, h, nz) > 227 * 1024 - 64) return false;
+            const int occ = cluster_occupancy(wp, h, nz);
+            return occ > 0 && (n + occ - 1) / occ <= rounds;
+        };
+        if (adjp && opt_kacc) {
+            ClusterGeom gk = g;
+            gk.kacc = 1;
+            if (fits(gk)) g.kacc = 1;
+        }
         if (adjp && opt_stage && opt_ckpt == CKPT_F32) {
             ClusterGeom gs = g;
             gs.stage = 1;
-            if (cluster_smem_bytes(wp, gs, nz) <= 227 * 1024 - 64 &&
-                cluster_occupancy(wp, gs, nz) >= cluster_occupancy(wp, g, nz))
-                g.stage = 1;
+            if (fits(gs)) g.stage = 1;
         }
         // the same values as every slot's (fill_slots)
         g.nx = nx;
@@ -983,6 +995,7 @@ int Solver::run_cluster_pass(int kind, int n) {
         }
         stats.tile_tz = -g.R;
         stats.tile_tx = g.cols_per;
+        if (adjp) stats.cluster_adj = (g.stage ? 1 : 0) | (g.kacc ? 2 : 0);
     }
     GB_CUDA_TRY(cudaEventRecord(ev_pass1, st));
     GB_CUDA_TRY(cudaStreamSynchronize(st));

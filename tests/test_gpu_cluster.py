@@ -78,17 +78,19 @@ def test_cluster_sizes_match_step_kernels(gpu, orc, wave, nx, size):
 
 
 @pytest.mark.parametrize("wave,nx,nz", [("sh", 681, 141), ("psv", 150, 110)])
-def test_cluster_checkpoint_staging_identical(gpu, orc, wave, nx, nz):
+def test_cluster_adjoint_shared_memory_options_identical(gpu, orc, wave, nx, nz):
     """The adjoint's kernel accumulation gives the same bits whether each
-    checkpoint is staged in shared memory or read from HBM."""
+    checkpoint is staged in shared memory or read from HBM, and whether the
+    shot's kernels are accumulated in shared memory or in an HBM buffer."""
     case = cases.make_case(wave=wave, nx=nx, nz=nz, nt=200, nsrc=2, nrec=min(nx - 4, 60), sfe=10, seed=nz)
     rng = np.random.default_rng(3)
     ad = [{c: (rng.standard_normal((case["nrec"], 200)) * 1e-3).astype(np.float32) for c in "xyz"}
           for _ in range(2)]
-    out = []
-    for stage in (1, 0):
+    out, used = [], set()
+    for stage, kacc in ((1, 1), (1, 0), (0, 1), (0, 0)):
         cfg, sol = cases.gpu_solver(gpu, case)
         sol.set_option("cluster_stage", stage)
+        sol.set_option("cluster_kacc", kacc)
         shots = [0, 1]
         sol.run_forward_batch(shots)
         for b in shots:
@@ -96,10 +98,17 @@ def test_cluster_checkpoint_staging_identical(gpu, orc, wave, nx, nz):
                 sol.set_adstf(c, ad[b][c], slot=b)
         sol.initKernels()
         sol.run_adjoint_batch(shots)
-        assert sol.stats().tile_tz < 0
+        st = sol.stats()
+        assert st.tile_tz < 0
+        assert st.cluster_adj & ~(stage | 2 * kacc) == 0
+        used.add(st.cluster_adj)
         out.append(sol.kernels())
-    for n in names(wave):
-        np.testing.assert_array_equal(out[0][n], out[1][n])
+        sol.close()
+    assert 2 in used or 3 in used, "no pass accumulated its kernels in shared memory"
+    assert 0 in used
+    for o in out[1:]:
+        for n in names(wave):
+            np.testing.assert_array_equal(o[n], out[0][n])
 
 
 def test_cluster_adjoint_matches_oracle(gpu, orc):
