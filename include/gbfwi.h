@@ -143,7 +143,10 @@ int gb_solver_batch_capacity(gb_solver *s);
  * stages each checkpoint in shared memory before the kernel accumulation when
  * it fits; 0: reads it from HBM, default), "cluster_kacc" (1: a cluster
  * adjoint keeps each shot's kernels in shared memory for the whole pass when
- * they fit, default; 0: adds into an HBM buffer), "cluster_qm" (columns per
+ * they fit, default; 0: adds into an HBM buffer), "cluster_shift" (1: the
+ * cluster pass shifts the rows of each thread group's columns in shared
+ * memory so that no warp meets bank conflicts, when it fits, default; 0:
+ * unshifted rows), "cluster_qm" (columns per
  * thread of the cluster pass: 0 = chosen with the cluster size, or 4, 8, 10,
  * 12, 16, 20, 24), "hbm_budget_gb". Options
  * change no forward result; "ckpt" changes kernels by the checkpoint
@@ -157,7 +160,9 @@ int gb_solver_set_option(gb_solver *s, const char *key, double value);
  * a cluster-resident pass of R-CTA clusters); march_bulk: 1 when the last
  * marching-kernel pass loaded its columns with bulk tensor copies;
  * cluster_adj: shared-memory use of the last cluster-resident adjoint pass,
- * bit 0 checkpoints staged, bit 1 kernels accumulated there. */
+ * bit 0 checkpoints staged, bit 1 kernels accumulated there; cluster_shift:
+ * row shift between thread groups in the last cluster-resident pass's
+ * shared-memory layout (0: unshifted). */
 typedef struct {
     double forward_ms, adjoint_ms, misfit_ms, filter_ms;
     double step_ms;
@@ -166,7 +171,7 @@ typedef struct {
     long long cell_updates;
     int tile_tz, tile_tx, batch_capacity;
     int march_bulk;
-    int cluster_adj;
+    int cluster_adj, cluster_shift;
 } gb_stats;
 int gb_solver_stats(gb_solver *s, gb_stats *out, int reset);
 

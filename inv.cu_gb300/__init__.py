@@ -59,7 +59,7 @@ class GbStats(ctypes.Structure):
                 ("step_ms", ctypes.c_double), ("step_launches", ctypes.c_longlong),
                 ("launches", ctypes.c_longlong), ("cell_updates", ctypes.c_longlong),
                 ("tile_tz", ctypes.c_int), ("tile_tx", ctypes.c_int), ("batch_capacity", ctypes.c_int),
-                ("march_bulk", ctypes.c_int), ("cluster_adj", ctypes.c_int)]
+                ("march_bulk", ctypes.c_int), ("cluster_adj", ctypes.c_int), ("cluster_shift", ctypes.c_int)]
 
 
 _lib = None

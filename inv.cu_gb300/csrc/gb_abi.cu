@@ -313,6 +313,8 @@ int gb_solver_set_option(gb_solver *s, const char *key, double value) {
         v.opt_stage = value != 0;
     } else if (k == "cluster_kacc") {
         v.opt_kacc = value != 0;
+    } else if (k == "cluster_shift") {
+        v.opt_shift = value != 0;
     } else if (k == "tma") {
         v.opt_tma = value != 0;
         v.invalidate_graphs();
@@ -357,9 +359,10 @@ int gb_solver_stats(gb_solver *s, gb_stats *out, int reset) {
     if (out) *out = s->s.stats;
     if (reset) {
         const int tz = s->s.stats.tile_tz, tx = s->s.stats.tile_tx, cap = s->s.stats.batch_capacity;
-        const int bulk = s->s.stats.march_bulk, cadj = s->s.stats.cluster_adj;
+        const int bulk = s->s.stats.march_bulk, cadj = s->s.stats.cluster_adj, csh = s->s.stats.cluster_shift;
         s->s.stats = gb_stats{};
         s->s.stats.cluster_adj = cadj;
+        s->s.stats.cluster_shift = csh;
         s->s.stats.tile_tz = tz;
         s->s.stats.tile_tx = tx;
         s->s.stats.batch_capacity = cap;

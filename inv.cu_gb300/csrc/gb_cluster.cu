@@ -49,8 +49,39 @@ __host__ __device__ constexpr int cluster_threads_for(bool psv, int qm) {
 
 int cluster_max_threads(bool psv, int qm) { return cluster_threads_for(psv, qm); }
 
-// Row stride of a shared-memory field: cp + 4 columns, made odd.
-__host__ __device__ inline int cluster_row_stride(int cp) { return (cp + 4) | 1; }
+// Shared-memory layout of the fields (see k_cluster): the row stride rs and
+// the row shift dshift between the column blocks of consecutive thread
+// groups. A warp whose lanes span two groups (rows a .. nz-1 of group g, rows
+// 0 .. of group g+1, QM columns further right) hits 32 distinct banks when,
+// with r = rs mod 32 odd, dshift = nz - QM * r^-1 (mod 32); among the odd rs
+// in [cp+4, cp+35] the one with the smallest field size is taken. Without
+// the shift (shift false, nz a multiple of 32, nz < 32 or a single group)
+// rs = (cp+4) | 1 and the straddling warps see two-way conflicts.
+void cluster_layout(ClusterGeom &g, int nz, bool shift) {
+    const int cp = g.cols_per, G = g.G;
+    g.rs = (cp + 4) | 1;
+    g.dshift = 0;
+    if (!shift || G < 2 || nz < 32 || nz % 32 == 0) return;
+    long best = -1;
+    for (int rs = cp + 4; rs < cp + 36; rs++) {
+        if (rs % 2 == 0) continue;
+        int rinv = 1;  // inverse of rs mod 32 (odd numbers are units)
+        while ((rinv * (rs % 32)) % 32 != 1) rinv += 2;
+        int d = ((nz - g.qmax * rinv) % 32 + 32) % 32;
+        if (d > 16) d -= 32;
+        const long size = (long)(nz + 4 + (G - 1) * std::abs(d)) * rs;
+        if (best < 0 || size < best) {
+            best = size;
+            g.rs = rs;
+            g.dshift = d;
+        }
+    }
+}
+
+// rows of one shared-memory field: nz + 4 plus the groups' row shifts
+__host__ __device__ inline int cluster_field_rows(int nz, int G, int dshift) {
+    return nz + 4 + (G - 1) * (dshift < 0 ? -dshift : dshift);
+}
 
 __device__ __forceinline__ uint32_t cl_mapa(uint32_t addr, uint32_t rank) {
     uint32_t r;
@@ -76,10 +107,15 @@ __device__ __forceinline__ void cp_async4_zf(float *dst, const float *src, bool 
 
 // Shared-memory field order. P-SV: vx vz ux uz sxx szz sxz; SH: vy uy sxy szy.
 // Each field is stored by rows (x fastest) with two zero pad rows above and
-// below it: field f, row j (-2 .. nz+1), local column c (-2 .. cp+1) at
-// sm[f*fs + (j+2)*rs + c + 2], fs = (nz+4)*rs. The row stride rs >= cp + 4 is
-// odd, so that a warp of consecutive rows hits 32 distinct banks, and a
-// thread's consecutive columns are immediate offsets from one address.
+// below it: field f, row j (-2 .. nz+1), local column c (-2 .. cp+1) of
+// thread group h (c / QM; the ghost columns go with the group beside them) at
+// sm[f*fs + (j + 2 + sigma_h)*rs + c + 2], sigma_h = sigma_0 + h*dshift >= 0,
+// fs = cluster_field_rows(nz, G, dshift)*rs. The row stride rs >= cp + 4 is
+// odd, so that a warp of consecutive rows of one group hits 32 distinct
+// banks, and a thread's consecutive columns are immediate offsets from one
+// address; the row shift makes warps that span two groups conflict-free too
+// (cluster_layout). Reads of the two columns on either side of a thread's
+// block add the row offset between the groups.
 //
 // cp is a multiple of QM and every thread updates QM columns; in the last CTA
 // the columns past the grid are updated too (never read by a grid column:
@@ -103,8 +139,9 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
     const size_t ncell = (size_t)nx * nz;
     const int x0 = rank * cp;
     const int ncols = min(cp, nx - x0);  // grid columns of this CTA, >= 2
-    const int rs = cluster_row_stride(cp);
-    const int fs = (nz + 4) * rs;  // one field
+    const int rs = g.rs, G = g.G, dsh = g.dshift;
+    const int fs = cluster_field_rows(nz, G, dsh) * rs;  // one field
+    const int sig0 = dsh < 0 ? -(G - 1) * dsh : 0;        // row shift of group 0
     const int t = threadIdx.x, j = t % nz, grp = t / nz;
     const int cb = grp * QM;                     // first local column of this thread
     const int nq = max(0, min(QM, ncols - cb));  // of which grid columns
@@ -179,11 +216,15 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
     const float dt = g.dt, c9x = g.c9x, c24x = g.c24x, c9z = g.c9z, c24z = g.c24z;
     const bool zS = j >= 2 && j < nz - 2, zV = j >= 1 && j < nz - 2;
     const int base_ck = (PSV && S.sh[0] != nullptr) ? 2 : 0;  // checkpoint field offset of this system
-    float *const P = sm + (j + 2) * rs + cb + 2;             // field 0, row j, column cb
-    // neighbours' shared memory: cluster address of their field 0, row j, column -2
-    const uint32_t me = (uint32_t)__cvta_generic_to_shared(sm + (j + 2) * rs);
-    const uint32_t lf = rank > 0 ? cl_mapa(me, rank - 1) : 0u;
-    const uint32_t rt = rank < R - 1 ? cl_mapa(me, rank + 1) : 0u;
+    float *const P = sm + (j + 2 + sig0 + grp * dsh) * rs + cb + 2;  // field 0, row j, column cb
+    // neighbours' shared memory: cluster address of their field 0, row j,
+    // column -2, in the rows of their last group (left neighbour, whose
+    // columns cp, cp+1 this CTA writes) or first group (right neighbour)
+    const uint32_t lf =
+        rank > 0 ? cl_mapa((uint32_t)__cvta_generic_to_shared(sm + (j + 2 + sig0 + (G - 1) * dsh) * rs), rank - 1)
+                 : 0u;
+    const uint32_t rt =
+        rank < R - 1 ? cl_mapa((uint32_t)__cvta_generic_to_shared(sm + (j + 2 + sig0) * rs), rank + 1) : 0u;
     // the thread owning columns 0, 1 sends them left; the one owning columns
     // cp-2, cp-1 sends them right (a CTA with a right neighbour holds cp columns)
     const bool edge_l = rank > 0 && grp == 0, edge_r = rank < R - 1 && cb + QM == cp;
@@ -245,7 +286,8 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
     prefetch(0);
 
     unsigned rb = (unsigned)rbase, sq = (unsigned)srcq, qn = (unsigned)nq;
-    unsigned fl = (edge_l ? 1u : 0u) | (edge_r ? 2u : 0u) | (zS ? 4u : 0u) | (zV ? 8u : 0u);
+    unsigned fl = (edge_l ? 1u : 0u) | (edge_r ? 2u : 0u) | (zS ? 4u : 0u) | (zV ? 8u : 0u) | (grp > 0 ? 16u : 0u) |
+                  (grp < G - 1 ? 32u : 0u);
     unsigned spm = spmask;
     for (int it = 0; it < nt; it++) {
         // The per-column conditions below are invariant over the time loop;
@@ -255,6 +297,10 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
         asm volatile("" : "+r"(sq), "+r"(qn), "+r"(fl), "+r"(spm));
         const int nq = (int)qn, srcq = (int)sq, rbase = (int)rb;
         const bool eL = fl & 1u, eR = fl & 2u, zs = fl & 4u, zv = fl & 8u;
+        // offsets (elements) from P's row to row j of the columns left of cb
+        // (group grp-1) and right of cb+QM-1 (group grp+1); ghost columns
+        // share the row shift of the group beside them
+        const int dl = (fl & 16u) ? -g.dshift * g.rs : 0, dr = (fl & 32u) ? g.dshift * g.rs : 0;
         if (spm) cp_async_wait_all();  // this step's injection
         // ---- phase A: divergence, sources, velocity, displacement
         {
@@ -262,14 +308,14 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
 #pragma unroll
             for (int w = 0; w < NWA; w++) {
                 const float *p = P + (FS + 2 * w) * fs;
-                wa[w][0] = p[-2];
-                wa[w][1] = p[-1];
+                wa[w][0] = p[dl - 2];
+                wa[w][1] = p[dl - 1];
                 wa[w][2] = p[0];
             }
 #pragma unroll
             for (int q = 0; q < QM; q++) {
 #pragma unroll
-                for (int w = 0; w < NWA; w++) wa[w][3] = P[(FS + 2 * w) * fs + q + 1];
+                for (int w = 0; w < NWA; w++) wa[w][3] = P[(FS + 2 * w) * fs + q + 1 + (q == QM - 1 ? dr : 0)];
                 const bool xS = (xs_mask >> q) & 1;
                 // ds = 0; ds = (x part) where xS; ds += (z part) where zS  (gb_stencil.h order)
                 float ds[NV];
@@ -371,7 +417,7 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
 #pragma unroll
             for (int f = 0; f < NV; f++) {
                 const float *p = P + (FV + f) * fs;
-                wb[f][0] = p[-1];
+                wb[f][0] = p[dl - 1];
                 wb[f][1] = p[0];
                 wb[f][2] = p[1];
             }
@@ -382,7 +428,7 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
 #pragma unroll
                 for (int f = 0; f < NV; f++) {
                     const float *v0 = P + (FV + f) * fs + q;
-                    wb[f][3] = v0[2];
+                    wb[f][3] = v0[2 + (q >= QM - 2 ? dr : 0)];
                     const float gx = st_dplus(wb[f][2], wb[f][1], wb[f][3], wb[f][0], c9x, c24x);
                     const float gz = st_dplus(v0[rs], wb[f][1], v0[2 * rs], v0[-rs], c9z, c24z);
                     dxv[f] = xV ? gx : 0.f;
@@ -513,7 +559,10 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
                             zm1 = __ldg(uc + zm);
                         }
                         const float *u0 = P + (FU + f) * fs + q;
-                        ux[f] = gx ? st_dplus(u0[1], u0[0], u0[2], u0[-1], c9x, c24x) : 0.f;
+                        const float um1 = q == 0 ? u0[dl - 1] : u0[-1];
+                        const float up1 = q == QM - 1 ? u0[dr + 1] : u0[1];
+                        const float up2 = q >= QM - 2 ? u0[dr + 2] : u0[2];
+                        ux[f] = gx ? st_dplus(up1, u0[0], up2, um1, c9x, c24x) : 0.f;
                         uzz[f] = zv ? st_dplus(u0[rs], u0[0], u0[2 * rs], u0[-rs], c9z, c24z) : 0.f;
                         fx[f] = gx ? st_dplus(cw[f][2], cw[f][1], cw[f][3], cw[f][0], c9x, c24x) : 0.f;
                         fz[f] = zv ? st_dplus(z1, cw[f][1], z2, zm1, c9z, c24z) : 0.f;
@@ -579,7 +628,7 @@ size_t cluster_smem_bytes(bool psv, const ClusterGeom &g, int nz) {
     const int nv = psv ? 2 : 1;
     const size_t stage = g.stage ? (size_t)nv * (2 * g.cols_per + 3) * nz : 0;
     const size_t kacc = g.kacc ? (size_t)(psv ? 3 : 2) * g.cols_per * nz : 0;
-    return ((size_t)(psv ? 7 : 4) * cluster_row_stride(g.cols_per) * (nz + 4) + (g.cols_per + 4) + g.nrec_cta +
+    return ((size_t)(psv ? 7 : 4) * g.rs * cluster_field_rows(nz, g.G, g.dshift) + (g.cols_per + 4) + g.nrec_cta +
             (size_t)(g.nrec_cta + 1) * nv + stage + kacc) *
            4;
 }

@@ -97,6 +97,7 @@ TileCfg tile_config(int id);
 // step and stencil coefficients), which the kernel reads from its parameters.
 struct ClusterGeom {
     int R, cols_per, G, qmax, nrec_cta;
+    int rs, dshift;  // shared-memory row stride; row shift between consecutive thread groups
     int stage;  // adjoint: stage each checkpoint in shared memory before the kernel accumulation
     int kacc;   // adjoint: accumulate the shot's kernels in shared memory, stored once after the pass
     int nx, nz, nt;
@@ -145,6 +146,7 @@ cudaError_t launch_fill(float *p, float v, size_t n, cudaStream_t st);
 // Cluster-resident passes (gb_cluster.cu): one cluster per slot runs the
 // whole pass; the adjoint adds each slot's kernels to kpart[slot][3][nx*nz].
 size_t cluster_smem_bytes(bool psv, const ClusterGeom &g, int nz);
+void cluster_layout(ClusterGeom &g, int nz, bool shift);
 int cluster_max_threads(bool psv, int qmax);
 int cluster_occupancy(bool psv, ClusterGeom g, int nz);
 cudaError_t launch_cluster(bool psv, bool adj, const Slot *d_slots, int nslots, ClusterGeom g, int nz, float *kpart,

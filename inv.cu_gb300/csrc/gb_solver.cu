@@ -178,6 +178,7 @@ int Solver::init(const Config &cfg, int nx_, int nz_, float xmax_, float zmax_) 
     if (cfg.has("cluster_qm")) opt_cluster_qm = cfg.iv("cluster_qm");
     if (cfg.has("cluster_stage")) opt_stage = cfg.iv("cluster_stage") != 0;
     if (cfg.has("cluster_kacc")) opt_kacc = cfg.iv("cluster_kacc") != 0;
+    if (cfg.has("cluster_shift")) opt_shift = cfg.iv("cluster_shift") != 0;
     if (cfg.has("cluster")) opt_cluster = std::max(0, std::min(16, cfg.iv("cluster")));
     nx = nx_;
     nz = nz_;
@@ -867,7 +868,8 @@ int Solver::run_pass(int kind, int n, bool snapshot, int snap_isrc) {
 // allowance) times the number of cluster rounds the batch needs.
 bool Solver::cluster_geometry(bool wave_psv, int n, ClusterGeom *out) const {
     if (nx < 2 || nz < 1) return false;
-    const long long key = (((long long)n * 32 + opt_cluster) * 32 + opt_cluster_qm) * 2 + (wave_psv ? 1 : 0);
+    const long long key =
+        ((((long long)n * 32 + opt_cluster) * 32 + opt_cluster_qm) * 2 + (wave_psv ? 1 : 0)) * 2 + (opt_shift ? 1 : 0);
     const auto hit = cluster_cache.find(key);
     if (hit != cluster_cache.end()) {
         if (hit->second.first) *out = hit->second.second;
@@ -891,29 +893,34 @@ bool Solver::cluster_geometry(bool wave_psv, int n, ClusterGeom *out) const {
                 if (rec_xi[r] >= 0 && rec_xi[r] < nx && rec_zi[r] >= 0 && rec_zi[r] < nz)
                     per[rec_xi[r] / g.cols_per]++;
             g.nrec_cta = *std::max_element(per.begin(), per.end());
-            if (cluster_smem_bytes(wave_psv, g, nz) > limit) continue;
-            const int occ = cluster_occupancy(wave_psv, g, nz);
-            if (occ < 1) {
+            // with the row-shifted layout first (conflict-free shared
+            // accesses; ties keep it), then without
+            for (int shifted = opt_shift ? 1 : 0; shifted >= 0; shifted--) {
+                cluster_layout(g, nz, shifted != 0);
+                if (cluster_smem_bytes(wave_psv, g, nz) > limit) continue;
+                const int occ = cluster_occupancy(wave_psv, g, nz);
+                if (occ < 1) {
+                    if (trace)
+                        std::fprintf(stderr, "gbfwi cluster %s R=%d cols=%d qmax=%d threads=%d shift=%d smem=%zu: no fit\n",
+                                     wave_psv ? "psv" : "sh", R, g.cols_per, g.qmax, g.G * nz, g.dshift,
+                                     cluster_smem_bytes(wave_psv, g, nz));
+                    continue;
+                }
+                // per-step time ~ cells per SM (CTAs sharing an SM add up) plus a
+                // barrier allowance, times the rounds the batch needs
+                const int resident = std::min(n, occ);
+                const int per_sm = (R * resident + num_sms - 1) / num_sms;
+                const double cost =
+                    (double)((n + occ - 1) / occ) * ((double)std::max(per_sm, 1) * g.cols_per * nz + 6000.0);
                 if (trace)
-                    std::fprintf(stderr, "gbfwi cluster %s R=%d cols=%d qmax=%d threads=%d smem=%zu: no fit\n",
-                                 wave_psv ? "psv" : "sh", R, g.cols_per, g.qmax, g.G * nz,
-                                 cluster_smem_bytes(wave_psv, g, nz));
-                continue;
-            }
-            // per-step time ~ cells per SM (CTAs sharing an SM add up) plus a
-            // barrier allowance, times the rounds the batch needs
-            const int resident = std::min(n, occ);
-            const int per_sm = (R * resident + num_sms - 1) / num_sms;
-            const double cost =
-                (double)((n + occ - 1) / occ) * ((double)std::max(per_sm, 1) * g.cols_per * nz + 6000.0);
-            if (trace)
-                std::fprintf(stderr,
-                             "gbfwi cluster %s R=%d cols=%d qmax=%d threads=%d smem=%zu clusters=%d cost=%.0f\n",
-                             wave_psv ? "psv" : "sh", R, g.cols_per, g.qmax, g.G * nz,
-                             cluster_smem_bytes(wave_psv, g, nz), occ, cost);
-            if (best < 0 || cost < best) {
-                best = cost;
-                *out = g;
+                    std::fprintf(stderr,
+                                 "gbfwi cluster %s R=%d cols=%d qmax=%d threads=%d shift=%d smem=%zu clusters=%d cost=%.0f\n",
+                                 wave_psv ? "psv" : "sh", R, g.cols_per, g.qmax, g.G * nz, g.dshift,
+                                 cluster_smem_bytes(wave_psv, g, nz), occ, cost);
+                if (best < 0 || cost < best) {
+                    best = cost;
+                    *out = g;
+                }
             }
         }
     }
@@ -958,7 +965,12 @@ int Solver::run_cluster_pass(int kind, int n) {
         }
         // adjoint: keep the shot's kernels in shared memory for the whole
         // pass, and stage each checkpoint there, when that fits without
-        // adding cluster rounds for this batch (the accumulators first)
+        // adding cluster rounds for this batch (the accumulators first). The
+        // accumulators are left in HBM when they would take the shared memory
+        // past 200 KB: the L1 left beside it no longer holds the lines the
+        // accumulation's checkpoint reads share (C2: 13.75 against 13.13 us
+        // per adjoint step at 229 KB), and the row-shifted layout is worth
+        // more than the accumulators (14.08 us unshifted with them).
         const int occ0 = adjp ? std::max(1, cluster_occupancy(wp, g, nz)) : 1;
         const int rounds = (n + occ0 - 1) / occ0;
         auto fits = [&](const ClusterGeom &h) {
@@ -969,7 +981,7 @@ int Solver::run_cluster_pass(int kind, int n) {
         if (adjp && opt_kacc) {
             ClusterGeom gk = g;
             gk.kacc = 1;
-            if (fits(gk)) g.kacc = 1;
+            if (cluster_smem_bytes(wp, gk, nz) <= 200 * 1024 && fits(gk)) g.kacc = 1;
         }
         if (adjp && opt_stage && opt_ckpt == CKPT_F32) {
             ClusterGeom gs = g;
@@ -996,6 +1008,7 @@ int Solver::run_cluster_pass(int kind, int n) {
         stats.tile_tz = -g.R;
         stats.tile_tx = g.cols_per;
         if (adjp) stats.cluster_adj = (g.stage ? 1 : 0) | (g.kacc ? 2 : 0);
+        stats.cluster_shift = g.dshift;
     }
     GB_CUDA_TRY(cudaEventRecord(ev_pass1, st));
     GB_CUDA_TRY(cudaStreamSynchronize(st));

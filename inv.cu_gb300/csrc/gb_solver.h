@@ -70,6 +70,7 @@ struct Solver {
     int opt_cluster_qm = 0;  // cluster columns per thread (0: chosen with the cluster size)
     int opt_stage = 0;    // cluster adjoint: stage checkpoints in shared memory when they fit
     int opt_kacc = 1;     // cluster adjoint: accumulate the kernels in shared memory when they fit
+    int opt_shift = 1;    // cluster passes: row-shifted shared-memory layout (no bank conflicts) when it fits
     int opt_cluster = 1;  // cluster-resident passes: 0 never, 1 automatic R, 2..16 this cluster size
 
     // device buffers in the reference layout
