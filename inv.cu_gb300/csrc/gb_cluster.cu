@@ -559,9 +559,9 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
                             zm1 = __ldg(uc + zm);
                         }
                         const float *u0 = P + (FU + f) * fs + q;
-                        const float um1 = q == 0 ? u0[dl - 1] : u0[-1];
-                        const float up1 = q == QM - 1 ? u0[dr + 1] : u0[1];
-                        const float up2 = q >= QM - 2 ? u0[dr + 2] : u0[2];
+                        const float um1 = u0[(q == 0 ? dl : 0) - 1];
+                        const float up1 = u0[(q == QM - 1 ? dr : 0) + 1];
+                        const float up2 = u0[(q >= QM - 2 ? dr : 0) + 2];
                         ux[f] = gx ? st_dplus(up1, u0[0], up2, um1, c9x, c24x) : 0.f;
                         uzz[f] = zv ? st_dplus(u0[rs], u0[0], u0[2 * rs], u0[-rs], c9z, c24z) : 0.f;
                         fx[f] = gx ? st_dplus(cw[f][2], cw[f][1], cw[f][3], cw[f][0], c9x, c24x) : 0.f;

@@ -50,6 +50,9 @@ constexpr int kRing = 8;  // ring slots per thread: column p is read while p+1..
 // Bulk loads fill the same ring as kStages stages of kStageCols columns: one
 // tensor copy per field and stage ({T rows, kStageCols columns} box).
 constexpr int kStageCols = 4, kStages = kRing / kStageCols;
+// injection values (per component) of a tile's sources, read into shared
+// memory before the march; a tile with more takes the rest from HBM
+constexpr int kInjStage = 256;
 static_assert(kStageCols == TMAP_BOX_COLS, "bulk-load box width");
 
 // 4-byte async copy to shared address `d` (a 32-bit shared-window address);
@@ -111,7 +114,8 @@ struct MarchWords {
 
 template <bool PSV>
 __host__ __device__ constexpr int march_smem_words(int threads) {
-    return (kRing * MarchWords<PSV>::N + 2 * ((PSV ? 2 : 1) + (PSV ? 2 : 1))) * threads + 2 * 2 * (2 + 2) * 2;
+    return (kRing * MarchWords<PSV>::N + 2 * ((PSV ? 2 : 1) + (PSV ? 2 : 1))) * threads + 2 * 2 * (2 + 2) * 2 +
+           (PSV ? 2 : 1) * kInjStage;
 }
 
 // TMA = false: each thread stages its own row with 4-byte cp.async.
@@ -128,11 +132,14 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
     extern __shared__ __align__(128) float smem[];
     __shared__ __align__(8) unsigned long long s_bar[kStages];
     __shared__ int s_dead;
+    __shared__ int s_inj_meta[2];  // first trace entry and count of the staged injection values
     const int T = blockDim.x, O = T - 8;
     const int TP = T + 4;  // exchange rows padded by 2 on both sides
     float *ring = smem;                                  // [kRing][W::N][T]
     float *s_sz = ring + kRing * W::N * T;               // [2][NZS][TP]
     float *s_vz = s_sz + 2 * NZS * TP;                   // [2][NV][TP]
+    // [NV][kInjStage] behind s_vz (its address is recomputed where it is read)
+    auto inj_stage = [&]() { return smem + kRing * W::N * blockDim.x + 2 * (NZS + NV) * (blockDim.x + 4); };
 
     // Blocks run shot-minor (block b: shot b % nslots, tile b / nslots): the
     // same strip of every shot runs close together, so the model columns,
@@ -214,6 +221,29 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
     }
     int inj_next = inj_ptr < inj_end ? inj_local[inj_ptr] : 0x7fffffff;
     int rec_next = rec_ptr < rec_end ? rec_local[rec_ptr] : 0x7fffffff;
+    // this step's injection values of the tile's sources (trace order within
+    // each cell), loaded together now instead of one dependent load per
+    // column during the march (an adjoint with a receiver in every surface
+    // column waited on HBM at every column step)
+    {
+        const int e0 = inj_ptr < inj_end ? inj_tptr[inj_ptr] : 0;
+        const int n = inj_ptr < inj_end ? min(inj_tptr[inj_end] - e0, kInjStage) : 0;
+        if (t == 0) {
+            s_inj_meta[0] = e0;
+            s_inj_meta[1] = n;
+        }
+        float *s_inj = inj_stage();
+        for (int e = t; e < n; e += T) {
+            const int ks = inj_traces[e0 + e] * nt + it;
+            if (PSV) {
+                s_inj[e] = __ldg(S.inj_x + ks);
+                s_inj[kInjStage + e] = __ldg(S.inj_z + ks);
+            } else {
+                s_inj[e] = __ldg(S.inj_y + ks);
+            }
+        }
+    }
+    __syncthreads();
 
     // Issues the loads of column step p into ring slot `slot` (own row only).
     // Offsets are 32-bit (grids are limited to 2^29 cells); the shared
@@ -419,13 +449,23 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
             const int cl = pv - (c0 - 1);
             while (inj_next < (cl + 1) * VZ) {
                 if (t == inj_next - cl * VZ + 3) {
+                    // read back here (volatile) rather than held in registers
+                    // through the march: sources are rare cells
+                    const int e0 = *(volatile int *)&s_inj_meta[0], n = *(volatile int *)&s_inj_meta[1];
+                    const float *s_inj = inj_stage();
                     for (int e = inj_tptr[inj_ptr]; e < inj_tptr[inj_ptr + 1]; e++) {
-                        const int ks = inj_traces[e] * nt + it;
-                        if (PSV) {
-                            ds[0] += __ldg(S.inj_x + ks);
-                            ds[NV - 1] += __ldg(S.inj_z + ks);
+                        const int o = e - e0;
+                        if (o < n) {
+                            ds[0] += s_inj[o];
+                            if (PSV) ds[NV - 1] += s_inj[kInjStage + o];
                         } else {
-                            ds[0] += __ldg(S.inj_y + ks);
+                            const int ks = inj_traces[e] * nt + it;
+                            if (PSV) {
+                                ds[0] += __ldg(S.inj_x + ks);
+                                ds[NV - 1] += __ldg(S.inj_z + ks);
+                            } else {
+                                ds[0] += __ldg(S.inj_y + ks);
+                            }
                         }
                     }
                 }
