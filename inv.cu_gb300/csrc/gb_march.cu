@@ -50,9 +50,12 @@ constexpr int kRing = 8;  // ring slots per thread: column p is read while p+1..
 // Bulk loads fill the same ring as kStages stages of kStageCols columns: one
 // tensor copy per field and stage ({T rows, kStageCols columns} box).
 constexpr int kStageCols = 4, kStages = kRing / kStageCols;
-// injection values (per component) of a tile's sources, read into shared
-// memory before the march; a tile with more takes the rest from HBM
-constexpr int kInjStage = 256;
+// A tile's source and receiver lists (cells, trace ranges, receiver traces)
+// and this step's injection values are copied into shared memory before the
+// march when they hold at most kCsrStage entries and kInjStage / kCsrStage
+// traces; a tile with more walks the lists in global memory.
+constexpr int kInjStage = 256, kCsrStage = 256;
+constexpr int kCsrStageWords = 5 * kCsrStage + 2;
 static_assert(kStageCols == TMAP_BOX_COLS, "bulk-load box width");
 
 // 4-byte async copy to shared address `d` (a 32-bit shared-window address);
@@ -115,7 +118,7 @@ struct MarchWords {
 template <bool PSV>
 __host__ __device__ constexpr int march_smem_words(int threads) {
     return (kRing * MarchWords<PSV>::N + 2 * ((PSV ? 2 : 1) + (PSV ? 2 : 1))) * threads + 2 * 2 * (2 + 2) * 2 +
-           (PSV ? 2 : 1) * kInjStage;
+           (PSV ? 2 : 1) * kInjStage + kCsrStageWords;
 }
 
 // TMA = false: each thread stages its own row with 4-byte cp.async.
@@ -219,31 +222,61 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
         rec_tptr = c.tptr;
         rec_traces = c.traces;
     }
-    int inj_next = inj_ptr < inj_end ? inj_local[inj_ptr] : 0x7fffffff;
-    int rec_next = rec_ptr < rec_end ? rec_local[rec_ptr] : 0x7fffffff;
-    // this step's injection values of the tile's sources (trace order within
-    // each cell), loaded together now instead of one dependent load per
-    // column during the march (an adjoint with a receiver in every surface
-    // column waited on HBM at every column step)
+    // The tile's lists and this step's injection values go to shared memory
+    // (one round of loads now instead of dependent global loads at every
+    // column step that has a source or receiver: an adjoint with a receiver
+    // in every surface column waited on memory at each of them). When they
+    // fit, the list pointers below point at the copies, with entry and trace
+    // indices rebased to 0, so the march walks them unchanged.
     {
-        const int e0 = inj_ptr < inj_end ? inj_tptr[inj_ptr] : 0;
-        const int n = inj_ptr < inj_end ? min(inj_tptr[inj_end] - e0, kInjStage) : 0;
-        if (t == 0) {
-            s_inj_meta[0] = e0;
-            s_inj_meta[1] = n;
-        }
         float *s_inj = inj_stage();
-        for (int e = t; e < n; e += T) {
-            const int ks = inj_traces[e0 + e] * nt + it;
-            if (PSV) {
-                s_inj[e] = __ldg(S.inj_x + ks);
-                s_inj[kInjStage + e] = __ldg(S.inj_z + ks);
-            } else {
-                s_inj[e] = __ldg(S.inj_y + ks);
+        int *si_loc = reinterpret_cast<int *>(s_inj + NV * kInjStage);
+        int *si_tp = si_loc + kCsrStage, *sr_loc = si_tp + kCsrStage + 1;
+        int *sr_tp = sr_loc + kCsrStage, *sr_tr = sr_tp + kCsrStage + 1;
+        const int ni = inj_end - inj_ptr, nr = rec_end - rec_ptr;
+        const int i0 = ni > 0 ? inj_tptr[inj_ptr] : 0, ti = ni > 0 ? inj_tptr[inj_end] - i0 : 0;
+        const int r0 = nr > 0 ? rec_tptr[rec_ptr] : 0, tr = nr > 0 ? rec_tptr[rec_end] - r0 : 0;
+        const bool stage_i = ni > 0 && ni <= kCsrStage && ti <= kInjStage;  // uniform over the block
+        const bool stage_r = nr > 0 && nr <= kCsrStage && tr <= kCsrStage;
+        if (stage_i) {
+            for (int k = t; k < ni; k += T) si_loc[k] = inj_local[inj_ptr + k];
+            for (int k = t; k <= ni; k += T) si_tp[k] = inj_tptr[inj_ptr + k] - i0;
+            for (int e = t; e < ti; e += T) {
+                const int ks = inj_traces[i0 + e] * nt + it;
+                if (PSV) {
+                    s_inj[e] = __ldg(S.inj_x + ks);
+                    s_inj[kInjStage + e] = __ldg(S.inj_z + ks);
+                } else {
+                    s_inj[e] = __ldg(S.inj_y + ks);
+                }
             }
         }
+        if (stage_r) {
+            for (int k = t; k < nr; k += T) sr_loc[k] = rec_local[rec_ptr + k];
+            for (int k = t; k <= nr; k += T) sr_tp[k] = rec_tptr[rec_ptr + k] - r0;
+            for (int e = t; e < tr; e += T) sr_tr[e] = rec_traces[r0 + e];
+        }
+        if (t == 0) {
+            s_inj_meta[0] = stage_i ? 0 : i0;  // trace index of s_inj[0]
+            s_inj_meta[1] = stage_i ? ti : 0;  // staged values
+        }
+        __syncthreads();
+        if (stage_i) {
+            inj_local = si_loc;
+            inj_tptr = si_tp;
+            inj_ptr = 0;
+            inj_end = ni;
+        }
+        if (stage_r) {
+            rec_local = sr_loc;
+            rec_tptr = sr_tp;
+            rec_traces = sr_tr;
+            rec_ptr = 0;
+            rec_end = nr;
+        }
     }
-    __syncthreads();
+    int inj_next = inj_ptr < inj_end ? inj_local[inj_ptr] : 0x7fffffff;
+    int rec_next = rec_ptr < rec_end ? rec_local[rec_ptr] : 0x7fffffff;
 
     // Issues the loads of column step p into ring slot `slot` (own row only).
     // Offsets are 32-bit (grids are limited to 2^29 cells); the shared
