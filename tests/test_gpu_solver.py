@@ -161,6 +161,46 @@ def test_march_bulk_loads_identical_to_cp_async(gpu, orc, tile, wave):
         np.testing.assert_array_equal(k_b[name], k_t[name])
 
 
+@pytest.mark.parametrize("wave", ["psv", "sh"])
+@pytest.mark.parametrize("tile", [13, 19])
+def test_march_dense_and_duplicate_receivers_identical(gpu, orc, tile, wave):
+    """A block of 20x20 receivers (more entries than a tile copies into
+    shared memory, so those tiles walk their lists in global memory), sparse
+    surface receivers (copied lists, samples gathered in shared memory) and
+    duplicated receiver cells (several traces per cell): the marching kernel
+    gives the 2-D tile kernel's bits."""
+    h = 10.0
+    case = cases.make_case(wave=wave, nx=133, nz=76, nt=120, nsrc=2, nrec=1, seed=31, dx=h)
+    rec = [[(10 + a) * h, (5 + b) * h] for a in range(20) for b in range(20)]
+    rec += [[(40 + 2 * a) * h, 2 * h] for a in range(40)]
+    rec += [[(40 + 2 * a) * h, 2 * h] for a in range(0, 40, 7)] + [[12 * h, 7 * h]]
+    case["rec"] = rec
+    case["nrec"] = len(rec)
+    rng = np.random.default_rng(8)
+    ad = {c: (rng.standard_normal((case["nrec"], case["nt"])) * 1e-3).astype(np.float32) for c in "xyz"}
+
+    def run(t):
+        cfg, sol = cases.gpu_solver(gpu, case)
+        sol.set_option("cluster", 0)
+        sol.set_option("tile", t)
+        sol.run_forward_batch([0, 1])
+        tr = {c: sol.out(c, slot=1) for c in comps(wave)}
+        for c in comps(wave):
+            sol.set_adstf(c, ad[c], slot=0)
+            sol.set_adstf(c, ad[c], slot=1)
+        sol.initKernels()
+        sol.run_adjoint_batch([0, 1])
+        return tr, sol.kernels()
+
+    tr_m, k_m = run(tile)
+    tr_t, k_t = run(1)
+    for c in comps(wave):
+        assert np.abs(tr_m[c]).max() > 0
+        np.testing.assert_array_equal(tr_m[c], tr_t[c])
+    for name in kernel_names(wave):
+        np.testing.assert_array_equal(k_m[name], k_t[name])
+
+
 def test_graphs_and_eager_identical(gpu, orc):
     case = cases.make_case(wave="sh", nx=100, nz=64, nt=300, nsrc=2, nrec=20, seed=19)
     cfg, a = cases.gpu_solver(gpu, case)
