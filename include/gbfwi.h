@@ -146,7 +146,10 @@ int gb_solver_batch_capacity(gb_solver *s);
  * they fit, default; 0: adds into an HBM buffer), "cluster_shift" (1: the
  * cluster pass shifts the rows of each thread group's columns in shared
  * memory so that no warp meets bank conflicts, when it fits, default; 0:
- * unshifted rows), "cluster_qm" (columns per
+ * unshifted rows), "cluster_snap" (1: a cluster adjoint stores its state at
+ * every accumulation step and a separate kernel accumulates the kernels
+ * after the pass, when that state fits in a quarter of the free device
+ * memory, default; 0: accumulates in the pass), "cluster_qm" (columns per
  * thread of the cluster pass: 0 = chosen with the cluster size, or 4, 8, 10,
  * 12, 16, 20, 24), "hbm_budget_gb". Options
  * change no forward result; "ckpt" changes kernels by the checkpoint
@@ -160,7 +163,8 @@ int gb_solver_set_option(gb_solver *s, const char *key, double value);
  * a cluster-resident pass of R-CTA clusters); march_bulk: 1 when the last
  * marching-kernel pass loaded its columns with bulk tensor copies;
  * cluster_adj: shared-memory use of the last cluster-resident adjoint pass,
- * bit 0 checkpoints staged, bit 1 kernels accumulated there; cluster_shift:
+ * bit 0 checkpoints staged, bit 1 kernels accumulated there, bit 2 adjoint
+ * state stored and the kernels accumulated after the pass; cluster_shift:
  * row shift between thread groups in the last cluster-resident pass's
  * shared-memory layout (0: unshifted). */
 typedef struct {

@@ -122,7 +122,7 @@ __device__ __forceinline__ void cp_async4_zf(float *dst, const float *src, bool 
 // the x differences of the last two grid columns are masked off).
 template <bool PSV, bool ADJ, int QM>
 __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
-    k_cluster(const Slot *__restrict__ slots, ClusterGeom g, float *__restrict__ kpart) {
+    k_cluster(const Slot *__restrict__ slots, ClusterGeom g, float *__restrict__ kpart, float *__restrict__ snap) {
     constexpr int NV = PSV ? 2 : 1;
     constexpr int NF = PSV ? 7 : 4;
     constexpr int NSF = NF - 2 * NV;             // stress fields
@@ -465,6 +465,20 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
             }
         }
         cl.sync();
+        // ---- adjoint with snap: the adjoint state of the owned grid cells at
+        // each accumulation step, [slot][step][u fields, v fields][cell], for
+        // the kernel accumulation after the pass (k_snap_interaction). Own
+        // cells only, read before this thread's next write: no barrier.
+        if (ADJ && snap && S.ckpt && S.sfe > 0 && it % S.sfe == 0 && it / S.sfe < S.nsfe) {
+            float *sp = snap + ((size_t)slot * S.nsfe + it / S.sfe) * (2 * NV) * ncell + (size_t)i0 * nz + j;
+#pragma unroll 1
+            for (int q = 0; q < nq; q++)
+#pragma unroll
+                for (int f = 0; f < NV; f++) {
+                    sp[(size_t)f * ncell + (size_t)q * nz] = P[(FU + f) * fs + q];
+                    sp[(size_t)(NV + f) * ncell + (size_t)q * nz] = P[(FV + f) * fs + q];
+                }
+        }
         // ---- adjoint: kernel accumulation every sfe steps (solver/fdm.h:583-606)
         // FP32 checkpoints (the only precision this path takes), copied into
         // shared memory at the start of phase B when g.stage, else read from
@@ -474,7 +488,7 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
         // (staged), and a cell's differences are masked where the reference
         // skips them. The shared accumulators (g.kacc) or the per-shot kernel
         // buffer take the `-=`.
-        if (ADJ && S.ckpt && S.sfe > 0 && it % S.sfe == 0 && it / S.sfe < S.nsfe) {
+        if (ADJ && !snap && S.ckpt && S.sfe > 0 && it % S.sfe == 0 && it / S.sfe < S.nsfe) {
             const int isfe_a = it / S.sfe;
             const float ndt = (float)S.sfe * dt;
             const float *ckb = static_cast<const float *>(S.ckpt) + ((size_t)isfe_a * S.nf + base_ck) * ncell;
@@ -607,6 +621,73 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
     }
 }
 
+// Kernel accumulation of a cluster-resident adjoint pass from the adjoint
+// state it stored at every accumulation step (snap) and the forward
+// checkpoints (solver/fdm.h:583-606): for each cell, the differences and the
+// `k -= ... * ndt` sequence over the accumulation steps, in step order, of the
+// in-pass accumulation, so the per-shot kernels are bit-identical to it. One
+// thread per cell of one shot (blockIdx.y = slot); neighbour offsets are 0
+// where the reference skips the difference, so no read leaves the grid.
+template <bool PSV>
+__global__ void k_snap_interaction(const Slot *__restrict__ slots, const float *__restrict__ snap, ClusterGeom g,
+                                   float *__restrict__ kpart) {
+    constexpr int NV = PSV ? 2 : 1;
+    const int slot = blockIdx.y;
+    const Slot &S = slots[slot];
+    if (!S.active || !S.ckpt || S.sfe <= 0) return;
+    const int nx = g.nx, nz = g.nz;
+    const size_t ncell = (size_t)nx * nz;
+    const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= ncell) return;
+    const int i = (int)(k / nz), j = (int)(k % nz);
+    const bool gx = i >= 1 && i < nx - 2, zv = j >= 1 && j < nz - 2;
+    const long ox = gx ? nz : 0, oz = zv ? 1 : 0;
+    const float ndt = (float)S.sfe * g.dt, c9x = g.c9x, c24x = g.c24x, c9z = g.c9z, c24z = g.c24z;
+    const int base_ck = (PSV && S.sh[0] != nullptr) ? 2 : 0;
+    const int nacc = min(S.nsfe, (g.nt - 1) / S.sfe + 1);
+    float kl = 0.f, km = 0.f, kr = 0.f;
+#pragma unroll 2
+    for (int a = 0; a < nacc; a++) {
+        const float *ua = snap + ((size_t)slot * S.nsfe + a) * (2 * NV) * ncell + k;
+        const float *uf = static_cast<const float *>(S.ckpt) + ((size_t)a * S.nf + base_ck) * ncell + k;
+        float ux[NV], uzz[NV], fx[NV], fz[NV], vf[NV], va[NV];
+#pragma unroll
+        for (int f = 0; f < NV; f++) {
+            const float *u0 = ua + (size_t)f * ncell, *w0 = uf + (size_t)f * ncell;
+            ux[f] = gx ? st_dplus(u0[ox], u0[0], u0[2 * ox], u0[-ox], c9x, c24x) : 0.f;
+            uzz[f] = zv ? st_dplus(u0[oz], u0[0], u0[2 * oz], u0[-oz], c9z, c24z) : 0.f;
+            fx[f] = gx ? st_dplus(__ldg(w0 + ox), __ldg(w0), __ldg(w0 + 2 * ox), __ldg(w0 - ox), c9x, c24x) : 0.f;
+            fz[f] = zv ? st_dplus(__ldg(w0 + oz), __ldg(w0), __ldg(w0 + 2 * oz), __ldg(w0 - oz), c9z, c24z) : 0.f;
+            vf[f] = __ldg(uf + (size_t)(NV + f) * ncell);
+            va[f] = ua[(size_t)(NV + f) * ncell];
+        }
+        if (PSV) {
+            const float dvxdx = ux[0], dvxdz = uzz[0], dvzdx = ux[NV - 1], dvzdz = uzz[NV - 1];
+            const float fxdx = fx[0], fxdz = fz[0], fzdx = fx[NV - 1], fzdz = fz[NV - 1];
+            kr = kr - (vf[0] * va[0] + vf[NV - 1] * va[NV - 1]) * ndt;
+            km = km - (2.f * dvxdx * fxdx + 2.f * dvzdz * fzdz + (dvxdz + dvzdx) * (fzdx + fxdz)) * ndt;
+            kl = kl - ((dvxdx + dvzdz) * (fxdx + fzdz)) * ndt;
+        } else {
+            kr = kr - vf[0] * va[0] * ndt;
+            km = km - (ux[0] * fx[0] + uzz[0] * fz[0]) * ndt;
+        }
+    }
+    if (PSV) kpart[((size_t)slot * 3 + 0) * ncell + k] = kl;
+    kpart[((size_t)slot * 3 + 1) * ncell + k] = km;
+    kpart[((size_t)slot * 3 + 2) * ncell + k] = kr;
+}
+
+cudaError_t launch_snap_interaction(bool psv, const Slot *d_slots, int nslots, const float *snap, ClusterGeom g,
+                                    float *kpart, cudaStream_t st) {
+    const size_t ncell = (size_t)g.nx * g.nz;
+    const dim3 grid((unsigned)((ncell + 255) / 256), nslots);
+    if (psv)
+        k_snap_interaction<true><<<grid, 256, 0, st>>>(d_slots, snap, g, kpart);
+    else
+        k_snap_interaction<false><<<grid, 256, 0, st>>>(d_slots, snap, g, kpart);
+    return cudaGetLastError();
+}
+
 // k_c += sum over slots of kpart[slot][c], in slot order, for the inverted
 // parameters.
 __global__ void k_cluster_reduce(const float *__restrict__ kpart, int nslots, size_t ncell, float *kl, float *km,
@@ -675,7 +756,7 @@ static cudaLaunchConfig_t cluster_config(ClusterGeom g, int nz, int nslots, size
 }
 
 cudaError_t launch_cluster(bool psv, bool adj, const Slot *d_slots, int nslots, ClusterGeom g, int nz, float *kpart,
-                           cudaStream_t st) {
+                           float *snap, cudaStream_t st) {
     if (nslots <= 0) return cudaSuccess;
     void *kern = cluster_kernel(psv, adj, g.qmax);
     if (!kern) return cudaErrorInvalidValue;
@@ -684,7 +765,7 @@ cudaError_t launch_cluster(bool psv, bool adj, const Slot *d_slots, int nslots, 
     if (e != cudaSuccess) return e;
     cudaLaunchAttribute attr[1];
     cudaLaunchConfig_t cfg = cluster_config(g, nz, nslots, smem, st, attr);
-    void *args[] = {(void *)&d_slots, (void *)&g, (void *)&kpart};
+    void *args[] = {(void *)&d_slots, (void *)&g, (void *)&kpart, (void *)&snap};
     return cudaLaunchKernelExC(&cfg, kern, args);
 }
 

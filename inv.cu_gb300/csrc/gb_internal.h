@@ -150,7 +150,11 @@ void cluster_layout(ClusterGeom &g, int nz, bool shift);
 int cluster_max_threads(bool psv, int qmax);
 int cluster_occupancy(bool psv, ClusterGeom g, int nz);
 cudaError_t launch_cluster(bool psv, bool adj, const Slot *d_slots, int nslots, ClusterGeom g, int nz, float *kpart,
-                           cudaStream_t st);
+                           float *snap, cudaStream_t st);
+// the kernel accumulation of a cluster adjoint pass that stored its adjoint
+// state (snap) instead of accumulating in the pass
+cudaError_t launch_snap_interaction(bool psv, const Slot *d_slots, int nslots, const float *snap, ClusterGeom g,
+                                    float *kpart, cudaStream_t st);
 cudaError_t launch_cluster_reduce(const float *kpart, int nslots, size_t ncell, float *kl, float *km, float *kr,
                                   int inv_l, int inv_m, int inv_r, cudaStream_t st);
 cudaError_t launch_mesh2grid(float *lambda, float *mu, float *rho, const float *px, const float *pz,

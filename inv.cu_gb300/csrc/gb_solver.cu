@@ -179,6 +179,7 @@ int Solver::init(const Config &cfg, int nx_, int nz_, float xmax_, float zmax_) 
     if (cfg.has("cluster_stage")) opt_stage = cfg.iv("cluster_stage") != 0;
     if (cfg.has("cluster_kacc")) opt_kacc = cfg.iv("cluster_kacc") != 0;
     if (cfg.has("cluster_shift")) opt_shift = cfg.iv("cluster_shift") != 0;
+    if (cfg.has("cluster_snap")) opt_snap = cfg.iv("cluster_snap") != 0;
     if (cfg.has("cluster")) opt_cluster = std::max(0, std::min(16, cfg.iv("cluster")));
     nx = nx_;
     nz = nz_;
@@ -308,6 +309,7 @@ void Solver::release() {
     cudaFree(d_csr);
     cudaFree(d_rec_cells);
     cudaFree(kpart);
+    cudaFree(snapbuf);
     for (cudaEvent_t e : {ev_pass0, ev_pass1, ev_win0, ev_win1, ev_t0, ev_t1})
         if (e) cudaEventDestroy(e);
     if (st) cudaStreamDestroy(st);
@@ -955,6 +957,29 @@ int Solver::run_cluster_pass(int kind, int n) {
         }
         GB_CUDA_TRY(cudaMemsetAsync(kpart, 0, (size_t)n * 3 * nc * 4, st));
     }
+    // adjoint: store the adjoint state at every accumulation step and
+    // accumulate the kernels after the pass, in one fully parallel kernel,
+    // when the state of every step fits in a quarter of the free device
+    // memory (as much memory as the FP32 checkpoints); else accumulate in
+    // the pass, where each thread's columns wait on memory one after another
+    float *snap = nullptr;
+    if (adjp && opt_snap && nsfe > 0) {
+        const size_t need = (size_t)n * nsfe * (psv ? 4 : 2) * nc * 4;
+        if (need > snap_bytes) {
+            size_t free_b = 0, total_b = 0;
+            GB_CUDA_TRY(cudaStreamSynchronize(st));
+            cudaFree(snapbuf);
+            snapbuf = nullptr;
+            snap_bytes = 0;
+            if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && need <= free_b / 4) {
+                if (cudaMalloc(&snapbuf, need) == cudaSuccess)
+                    snap_bytes = need;
+                else
+                    (void)cudaGetLastError();
+            }
+        }
+        if (snap_bytes >= need) snap = snapbuf;
+    }
     for (int w = 0; w < 2; w++) {
         const bool wp = w == 1;
         if (wp ? !psv : !sh) continue;
@@ -971,19 +996,19 @@ int Solver::run_cluster_pass(int kind, int n) {
         // accumulation's checkpoint reads share (C2: 13.75 against 13.13 us
         // per adjoint step at 229 KB), and the row-shifted layout is worth
         // more than the accumulators (14.08 us unshifted with them).
-        const int occ0 = adjp ? std::max(1, cluster_occupancy(wp, g, nz)) : 1;
+        const int occ0 = (adjp && !snap) ? std::max(1, cluster_occupancy(wp, g, nz)) : 1;
         const int rounds = (n + occ0 - 1) / occ0;
         auto fits = [&](const ClusterGeom &h) {
             if (cluster_smem_bytes(wp, h, nz) > 227 * 1024 - 64) return false;
             const int occ = cluster_occupancy(wp, h, nz);
             return occ > 0 && (n + occ - 1) / occ <= rounds;
         };
-        if (adjp && opt_kacc) {
+        if (adjp && !snap && opt_kacc) {
             ClusterGeom gk = g;
             gk.kacc = 1;
             if (cluster_smem_bytes(wp, gk, nz) <= 200 * 1024 && fits(gk)) g.kacc = 1;
         }
-        if (adjp && opt_stage && opt_ckpt == CKPT_F32) {
+        if (adjp && !snap && opt_stage && opt_ckpt == CKPT_F32) {
             ClusterGeom gs = g;
             gs.stage = 1;
             if (fits(gs)) g.stage = 1;
@@ -997,8 +1022,12 @@ int Solver::run_cluster_pass(int kind, int n) {
         g.c24x = 1.f / (24.f * dx);
         g.c9z = 9.f / (8.f * dz);
         g.c24z = 1.f / (24.f * dz);
-        GB_CUDA_TRY(launch_cluster(wp, adjp, d_slots[kind], n, g, nz, adjp ? kpart : nullptr, st));
+        GB_CUDA_TRY(launch_cluster(wp, adjp, d_slots[kind], n, g, nz, adjp ? kpart : nullptr, snap, st));
         stats.launches += 1;
+        if (snap) {
+            GB_CUDA_TRY(launch_snap_interaction(wp, d_slots[kind], n, snap, g, kpart, st));
+            stats.launches += 1;
+        }
         if (adjp) {
             GB_CUDA_TRY(launch_cluster_reduce(kpart, n, nc, k_lambda, k_mu, k_rho, wp && inv_lambda, inv_mu, inv_rho,
                                               st));
@@ -1007,7 +1036,7 @@ int Solver::run_cluster_pass(int kind, int n) {
         }
         stats.tile_tz = -g.R;
         stats.tile_tx = g.cols_per;
-        if (adjp) stats.cluster_adj = (g.stage ? 1 : 0) | (g.kacc ? 2 : 0);
+        if (adjp) stats.cluster_adj = (g.stage ? 1 : 0) | (g.kacc ? 2 : 0) | (snap ? 4 : 0);
         stats.cluster_shift = g.dshift;
     }
     GB_CUDA_TRY(cudaEventRecord(ev_pass1, st));

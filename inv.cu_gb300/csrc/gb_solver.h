@@ -71,6 +71,7 @@ struct Solver {
     int opt_stage = 0;    // cluster adjoint: stage checkpoints in shared memory when they fit
     int opt_kacc = 1;     // cluster adjoint: accumulate the kernels in shared memory when they fit
     int opt_shift = 1;    // cluster passes: row-shifted shared-memory layout (no bank conflicts) when it fits
+    int opt_snap = 1;     // cluster adjoint: store the adjoint state, accumulate the kernels after the pass
     int opt_cluster = 1;  // cluster-resident passes: 0 never, 1 automatic R, 2..16 this cluster size
 
     // device buffers in the reference layout
@@ -83,6 +84,8 @@ struct Solver {
     bool rec_distinct = true;     // no two receivers share a cell
     float *kpart = nullptr;       // per-slot kernel contributions (cluster adjoint)
     size_t kpart_slots = 0;
+    float *snapbuf = nullptr;     // cluster adjoint state at each accumulation step
+    size_t snap_bytes = 0;
 
     // batch slots
     std::vector<SlotBuf> slots;

@@ -89,6 +89,7 @@ def test_cluster_adjoint_shared_memory_options_identical(gpu, orc, wave, nx, nz)
     out, used = [], set()
     for stage, kacc in ((1, 1), (1, 0), (0, 1), (0, 0)):
         cfg, sol = cases.gpu_solver(gpu, case)
+        sol.set_option("cluster_snap", 0)  # the in-pass accumulation's options
         sol.set_option("cluster_stage", stage)
         sol.set_option("cluster_kacc", kacc)
         shots = [0, 1]
@@ -124,6 +125,7 @@ def test_cluster_row_shift_identical(gpu, orc, wave, nx, nz):
     for shift, kacc in ((1, 1), (1, 0), (0, 1)):
         cfg, sol = cases.gpu_solver(gpu, case)
         sol.set_option("cluster_shift", shift)
+        sol.set_option("cluster_snap", 0)
         sol.set_option("cluster_kacc", kacc)
         shots = [0, 1]
         sol.run_forward_batch(shots)
@@ -142,6 +144,42 @@ def test_cluster_row_shift_identical(gpu, orc, wave, nx, nz):
     assert (shifts[0] != 0 or (nx, nz) == (94, 40)) and shifts[2] == 0
     for tr, k in out[1:]:
         for b in range(2):
+            for c in comps(wave):
+                np.testing.assert_array_equal(tr[b][c], out[0][0][b][c])
+        for n in names(wave):
+            np.testing.assert_array_equal(k[n], out[0][1][n])
+
+
+@pytest.mark.parametrize("wave,nx,nz", [("sh", 681, 141), ("psv", 200, 200), ("psv", 94, 40)])
+def test_cluster_adjoint_after_pass_identical(gpu, orc, wave, nx, nz):
+    """Kernels accumulated after the pass from the stored adjoint state equal,
+    bit for bit, those accumulated inside the pass (in shared memory or in
+    HBM), and the forward seismograms are unchanged."""
+    case = cases.make_case(wave=wave, nx=nx, nz=nz, nt=210, nsrc=3, nrec=min(nx - 4, 60), sfe=10, seed=nx - nz)
+    rng = np.random.default_rng(9)
+    ad = [{c: (rng.standard_normal((case["nrec"], 210)) * 1e-3).astype(np.float32) for c in "xyz"}
+          for _ in range(3)]
+    out, flags = [], []
+    for snap, kacc in ((1, 1), (0, 1), (0, 0)):
+        cfg, sol = cases.gpu_solver(gpu, case)
+        sol.set_option("cluster_snap", snap)
+        sol.set_option("cluster_kacc", kacc)
+        shots = [0, 1, 2]
+        sol.run_forward_batch(shots)
+        tr = [{c: sol.out(c, slot=b) for c in comps(wave)} for b in shots]
+        for b in shots:
+            for c in comps(wave):
+                sol.set_adstf(c, ad[b][c], slot=b)
+        sol.initKernels()
+        sol.run_adjoint_batch(shots)
+        st = sol.stats()
+        assert st.tile_tz < 0
+        flags.append(st.cluster_adj)
+        out.append((tr, sol.kernels()))
+        sol.close()
+    assert flags[0] & 4 and not flags[1] & 4 and not flags[2] & 4
+    for tr, k in out[1:]:
+        for b in range(3):
             for c in comps(wave):
                 np.testing.assert_array_equal(tr[b][c], out[0][0][b][c])
         for n in names(wave):
