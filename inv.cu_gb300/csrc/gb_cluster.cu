@@ -13,9 +13,12 @@
 //   barrier  (all velocities written, all stresses of step n still in place)
 //   phase B  velocity gradients and stress update
 //   barrier  (all stresses written before the next phase A reads them)
-// plus, in the adjoint, the kernel accumulation every sfe steps (one more
-// barrier; the shot's kernels stay in shared memory for the whole pass when
-// the CTA has room, and the checkpoint can be staged there during phase B). A thread that updates one of the CTA's edge columns also writes
+// plus, in the adjoint, every sfe steps either a store of the adjoint state
+// of the CTA's cells for the kernel accumulation after the pass
+// (k_snap_interaction), or the accumulation itself (one more barrier; the
+// shot's kernels stay in shared memory for the whole pass when the CTA has
+// room, and the checkpoint can be staged there during phase B). A thread
+// that updates one of the CTA's edge columns also writes
 // the new value into the neighbouring CTA's ghost column (st.shared::cluster,
 // made visible by the cluster barrier's release/acquire), so the stencils
 // only ever read the CTA's own shared memory. The x-differences walk the
@@ -24,10 +27,10 @@
 //
 // Every cell is computed with the operations, in the order, of the fused
 // step kernels (gb_stencil.h): forward traces and checkpoints are
-// bit-identical to theirs. The adjoint accumulates each shot's kernel
-// contribution in a per-shot buffer (directly, or from the shared-memory
-// accumulators at the end of the pass) that is added to the kernels after
-// the pass, in shot order.
+// bit-identical to theirs. Each shot's kernel contribution goes to a
+// per-shot buffer (from k_snap_interaction, directly from the in-pass
+// accumulation, or from its shared-memory accumulators at the end of the
+// pass) that is added to the kernels after the pass, in shot order.
 #include <cooperative_groups.h>
 
 #include <algorithm>
