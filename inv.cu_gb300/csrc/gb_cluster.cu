@@ -592,12 +592,12 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
                     if (PSV) {
                         const float dvxdx = ux[0], dvxdz = uzz[0], dvzdx = ux[NV - 1], dvzdz = uzz[NV - 1];
                         const float fxdx = fx[0], fxdz = fz[0], fzdx = fx[NV - 1], fzdz = fz[NV - 1];
-                        nr = ok[2] - (vf[0] * v0[0] + vf[NV - 1] * v0[fs]) * ndt;
-                        nm = ok[1] - (2.f * dvxdx * fxdx + 2.f * dvzdz * fzdz + (dvxdz + dvzdx) * (fzdx + fxdz)) * ndt;
-                        nl = ok[0] - ((dvxdx + dvzdz) * (fxdx + fzdz)) * ndt;
+                        nr = st_krho_psv(ok[2], vf[0], v0[0], vf[NV - 1], v0[fs], ndt);
+                        nm = st_kmu_psv(ok[1], dvxdx, dvxdz, dvzdx, dvzdz, fxdx, fxdz, fzdx, fzdz, ndt);
+                        nl = st_klambda_psv(ok[0], dvxdx, dvzdz, fxdx, fzdz, ndt);
                     } else {
-                        nr = ok[2] - vf[0] * v0[0] * ndt;
-                        nm = ok[1] - (ux[0] * fx[0] + uzz[0] * fz[0]) * ndt;
+                        nr = st_krho_sh(ok[2], vf[0], v0[0], ndt);
+                        nm = st_kmu_sh(ok[1], ux[0], fx[0], uzz[0], fz[0], ndt);
                     }
                     if (kin) {
                         ar[o] = nr;
@@ -627,8 +627,9 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
 // Kernel accumulation of a cluster-resident adjoint pass from the adjoint
 // state it stored at every accumulation step (snap) and the forward
 // checkpoints (solver/fdm.h:583-606): for each cell, the differences and the
-// `k -= ... * ndt` sequence over the accumulation steps, in step order, of the
-// in-pass accumulation, so the per-shot kernels are bit-identical to it. One
+// accumulation helpers (gb_stencil.h) of the in-pass accumulation, over the
+// accumulation steps in step order, so the per-shot kernels are
+// bit-identical to it. One
 // thread per cell of one shot (blockIdx.y = slot); neighbour offsets are 0
 // where the reference skips the difference, so no read leaves the grid.
 template <bool PSV>
@@ -656,23 +657,29 @@ __global__ void k_snap_interaction(const Slot *__restrict__ slots, const float *
         float ux[NV], uzz[NV], fx[NV], fz[NV], vf[NV], va[NV];
 #pragma unroll
         for (int f = 0; f < NV; f++) {
+            // every load is issued (the offsets are 0 where a difference is
+            // masked), so that the step's loads are all in flight together
             const float *u0 = ua + (size_t)f * ncell, *w0 = uf + (size_t)f * ncell;
-            ux[f] = gx ? st_dplus(u0[ox], u0[0], u0[2 * ox], u0[-ox], c9x, c24x) : 0.f;
-            uzz[f] = zv ? st_dplus(u0[oz], u0[0], u0[2 * oz], u0[-oz], c9z, c24z) : 0.f;
-            fx[f] = gx ? st_dplus(__ldg(w0 + ox), __ldg(w0), __ldg(w0 + 2 * ox), __ldg(w0 - ox), c9x, c24x) : 0.f;
-            fz[f] = zv ? st_dplus(__ldg(w0 + oz), __ldg(w0), __ldg(w0 + 2 * oz), __ldg(w0 - oz), c9z, c24z) : 0.f;
+            const float a0 = u0[0], axp = u0[ox], axp2 = u0[2 * ox], axm = u0[-ox];
+            const float azp = u0[oz], azp2 = u0[2 * oz], azm = u0[-oz];
+            const float b0 = __ldg(w0), bxp = __ldg(w0 + ox), bxp2 = __ldg(w0 + 2 * ox), bxm = __ldg(w0 - ox);
+            const float bzp = __ldg(w0 + oz), bzp2 = __ldg(w0 + 2 * oz), bzm = __ldg(w0 - oz);
+            ux[f] = gx ? st_dplus(axp, a0, axp2, axm, c9x, c24x) : 0.f;
+            uzz[f] = zv ? st_dplus(azp, a0, azp2, azm, c9z, c24z) : 0.f;
+            fx[f] = gx ? st_dplus(bxp, b0, bxp2, bxm, c9x, c24x) : 0.f;
+            fz[f] = zv ? st_dplus(bzp, b0, bzp2, bzm, c9z, c24z) : 0.f;
             vf[f] = __ldg(uf + (size_t)(NV + f) * ncell);
             va[f] = ua[(size_t)(NV + f) * ncell];
         }
         if (PSV) {
             const float dvxdx = ux[0], dvxdz = uzz[0], dvzdx = ux[NV - 1], dvzdz = uzz[NV - 1];
             const float fxdx = fx[0], fxdz = fz[0], fzdx = fx[NV - 1], fzdz = fz[NV - 1];
-            kr = kr - (vf[0] * va[0] + vf[NV - 1] * va[NV - 1]) * ndt;
-            km = km - (2.f * dvxdx * fxdx + 2.f * dvzdz * fzdz + (dvxdz + dvzdx) * (fzdx + fxdz)) * ndt;
-            kl = kl - ((dvxdx + dvzdz) * (fxdx + fzdz)) * ndt;
+            kr = st_krho_psv(kr, vf[0], va[0], vf[NV - 1], va[NV - 1], ndt);
+            km = st_kmu_psv(km, dvxdx, dvxdz, dvzdx, dvzdz, fxdx, fxdz, fzdx, fzdz, ndt);
+            kl = st_klambda_psv(kl, dvxdx, dvzdz, fxdx, fzdz, ndt);
         } else {
-            kr = kr - vf[0] * va[0] * ndt;
-            km = km - (ux[0] * fx[0] + uzz[0] * fz[0]) * ndt;
+            kr = st_krho_sh(kr, vf[0], va[0], ndt);
+            km = st_kmu_sh(km, ux[0], fx[0], uzz[0], fz[0], ndt);
         }
     }
     if (PSV) kpart[((size_t)slot * 3 + 0) * ncell + k] = kl;

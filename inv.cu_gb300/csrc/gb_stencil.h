@@ -38,4 +38,31 @@ __device__ __forceinline__ void st_stress_sh(float &sxy, float &szy, float m, fl
     szy = fmaf(dtm, dvydz, szy);
 }
 
+// Kernel accumulation (interaction*, solver/fdm.h:198-219): k - c ndt, the
+// contribution c formed in a fixed order (products feeding a sum are
+// __fmul_rn, which the compiler never fuses), so the in-pass, after-pass
+// and per-step forms give the same bits.
+// SH: k_rho -= v_fw v ndt
+__device__ __forceinline__ float st_krho_sh(float k, float vf, float va, float ndt) {
+    return fmaf(-__fmul_rn(vf, va), ndt, k);
+}
+// SH: k_mu -= (dx u dx u_fw + dz u dz u_fw) ndt
+__device__ __forceinline__ float st_kmu_sh(float k, float ux, float fx, float uz, float fz, float ndt) {
+    return fmaf(-fmaf(ux, fx, __fmul_rn(uz, fz)), ndt, k);
+}
+// P-SV: k_rho -= (vx vx_fw + vz vz_fw) ndt
+__device__ __forceinline__ float st_krho_psv(float k, float vf0, float va0, float vf1, float va1, float ndt) {
+    return fmaf(-fmaf(vf0, va0, __fmul_rn(vf1, va1)), ndt, k);
+}
+// P-SV: k_mu -= (2 dxux dxux_fw + 2 dzuz dzuz_fw + (dzux + dxuz)(dxuz_fw + dzux_fw)) ndt
+__device__ __forceinline__ float st_kmu_psv(float k, float dvxdx, float dvxdz, float dvzdx, float dvzdz, float fxdx,
+                                            float fxdz, float fzdx, float fzdz, float ndt) {
+    const float shear = __fmul_rn(dvxdz + dvzdx, fzdx + fxdz);
+    return fmaf(-fmaf(2.f * dvxdx, fxdx, fmaf(2.f * dvzdz, fzdz, shear)), ndt, k);
+}
+// P-SV: k_lambda -= (dxux + dzuz)(dxux_fw + dzuz_fw) ndt
+__device__ __forceinline__ float st_klambda_psv(float k, float dvxdx, float dvzdz, float fxdx, float fzdz, float ndt) {
+    return fmaf(-__fmul_rn(dvxdx + dvzdz, fxdx + fzdz), ndt, k);
+}
+
 }  // namespace gb

@@ -561,20 +561,19 @@ __global__ void k_interaction(const Slot *__restrict__ slots, const KernelGroup 
             if (G.inv_rho) {
                 const float vx_fw = ck_load(S, isfe, base + 2, k, n, inv[2]);
                 const float vz_fw = ck_load(S, isfe, base + 3, k, n, inv[3]);
-                kr -= (vx_fw * __ldg(S.psv[VX0 + par] + k) + vz_fw * __ldg(S.psv[VZ0 + par] + k)) * ndt;
+                kr = st_krho_psv(kr, vx_fw, __ldg(S.psv[VX0 + par] + k), vz_fw, __ldg(S.psv[VZ0 + par] + k), ndt);
             }
-            if (G.inv_mu)
-                km -= (2.f * dvxdx * fxdx + 2.f * dvzdz * fzdz + (dvxdz + dvzdx) * (fzdx + fxdz)) * ndt;
-            if (G.inv_lambda) kl -= ((dvxdx + dvzdz) * (fxdx + fzdz)) * ndt;
+            if (G.inv_mu) km = st_kmu_psv(km, dvxdx, dvxdz, dvzdx, dvzdz, fxdx, fxdz, fzdx, fzdz, ndt);
+            if (G.inv_lambda) kl = st_klambda_psv(kl, dvxdx, dvzdz, fxdx, fzdz, ndt);
         } else {
             float dvydx, dvydz, fdx, fdz;
             grad(S.sh[UY], dvydx, dvydz);
             grad_ck(0, fdx, fdz);
             if (G.inv_rho) {
                 const float vy_fw = ck_load(S, isfe, 1, k, n, inv[1]);
-                kr -= vy_fw * __ldg(S.sh[VY0 + par] + k) * ndt;
+                kr = st_krho_sh(kr, vy_fw, __ldg(S.sh[VY0 + par] + k), ndt);
             }
-            if (G.inv_mu) km -= (dvydx * fdx + dvydz * fdz) * ndt;
+            if (G.inv_mu) km = st_kmu_sh(km, dvydx, fdx, dvydz, fdz, ndt);
         }
     }
     if (G.inv_lambda) G.k_lambda[k] = kl;
