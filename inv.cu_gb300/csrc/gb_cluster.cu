@@ -233,10 +233,13 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
     const bool edge_l = rank > 0 && grp == 0, edge_r = rank < R - 1 && cb + QM == cp;
     const int nrq = __popc(rmask);
 
-    // checkpoint index written after step `step` (-1: none)
-    auto ckpt_of = [&](int step) -> int {
-        if (ADJ || !S.ckpt || S.sfe <= 0 || (step + 1) % S.sfe != 0) return -1;
-        return S.nsfe - (step + 1) / S.sfe;
+    // Steps are counted as it = blk * sfe + ph (sfe > 0), kept by increments
+    // instead of an integer division per step. Checkpoint index written after
+    // the step with counters (ph, blk) (-1: none).
+    const int sfe = S.sfe > 0 ? S.sfe : 1;
+    auto ckpt_at = [&](int ph, int blk) -> int {
+        if (ADJ || !S.ckpt || S.sfe <= 0 || ph != sfe - 1) return -1;
+        return S.nsfe - (blk + 1);
     };
     // owned grid cells of NV fields from field f0 to checkpoint field q0
     auto store_ckpt = [&](int isfe, int f0, int q0) {
@@ -285,13 +288,14 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
         }
     };
     cl.sync();
-    if (ckpt_of(0) >= 0) store_ckpt(ckpt_of(0), FU, 0);  // displacement before step 0
+    if (ckpt_at(0, 0) >= 0) store_ckpt(ckpt_at(0, 0), FU, 0);  // displacement before step 0
     prefetch(0);
 
     unsigned rb = (unsigned)rbase, sq = (unsigned)srcq, qn = (unsigned)nq;
     unsigned fl = (edge_l ? 1u : 0u) | (edge_r ? 2u : 0u) | (zS ? 4u : 0u) | (zV ? 8u : 0u) | (grp > 0 ? 16u : 0u) |
-                  (grp < G - 1 ? 32u : 0u);
+                  (grp < G - 1 ? 32u : 0u) | (S.record_u ? 64u : 0u);
     unsigned spm = spmask;
+    int ph = 0, blk = 0;  // it = blk * sfe + ph
     for (int it = 0; it < nt; it++) {
         // The per-column conditions below are invariant over the time loop;
         // hoisting them out of it would hold registers per owned column.
@@ -380,7 +384,7 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
                 }
                 if (!ADJ && e >= 0) {
 #pragma unroll
-                    for (int f = 0; f < NV; f++) rbuf[e * NV + f] = S.record_u ? un[f] : vn[f];
+                    for (int f = 0; f < NV; f++) rbuf[e * NV + f] = (fl & 64u) ? un[f] : vn[f];
                 }
 #pragma unroll
                 for (int w = 0; w < NWA; w++) {
@@ -407,13 +411,14 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
                     S.out_y[kr] = rbuf[e * NV];
                 }
             }
-            const int isfe = ckpt_of(it);
+            const int isfe = ckpt_at(ph, blk);
             if (isfe >= 0) store_ckpt(isfe, FV, NV);
-            const int isfe_n = it + 1 < nt ? ckpt_of(it + 1) : -1;
+            const bool wrap = ph + 1 == sfe;
+            const int isfe_n = it + 1 < nt ? ckpt_at(wrap ? 0 : ph + 1, wrap ? blk + 1 : blk) : -1;
             if (isfe_n >= 0) store_ckpt(isfe_n, FU, 0);
         }
         prefetch(it + 1);
-        if (ADJ && g.stage && S.ckpt && S.sfe > 0 && it % S.sfe == 0 && it / S.sfe < S.nsfe) stage_ckpt(it / S.sfe);
+        if (ADJ && g.stage && S.ckpt && S.sfe > 0 && ph == 0 && blk < S.nsfe) stage_ckpt(blk);
         // ---- phase B: velocity gradients and stress update
         {
             float wb[NV][4];  // x-window: columns c-1, c, c+1, c+2
@@ -472,8 +477,8 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
         // each accumulation step, [slot][step][u fields, v fields][cell], for
         // the kernel accumulation after the pass (k_snap_interaction). Own
         // cells only, read before this thread's next write: no barrier.
-        if (ADJ && snap && S.ckpt && S.sfe > 0 && it % S.sfe == 0 && it / S.sfe < S.nsfe) {
-            float *sp = snap + ((size_t)slot * S.nsfe + it / S.sfe) * (2 * NV) * ncell + (size_t)i0 * nz + j;
+        if (ADJ && snap && S.ckpt && S.sfe > 0 && ph == 0 && blk < S.nsfe) {
+            float *sp = snap + ((size_t)slot * S.nsfe + blk) * (2 * NV) * ncell + (size_t)i0 * nz + j;
 #pragma unroll 1
             for (int q = 0; q < nq; q++)
 #pragma unroll
@@ -491,8 +496,8 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
         // (staged), and a cell's differences are masked where the reference
         // skips them. The shared accumulators (g.kacc) or the per-shot kernel
         // buffer take the `-=`.
-        if (ADJ && !snap && S.ckpt && S.sfe > 0 && it % S.sfe == 0 && it / S.sfe < S.nsfe) {
-            const int isfe_a = it / S.sfe;
+        if (ADJ && !snap && S.ckpt && S.sfe > 0 && ph == 0 && blk < S.nsfe) {
+            const int isfe_a = blk;
             const float ndt = (float)S.sfe * dt;
             const float *ckb = static_cast<const float *>(S.ckpt) + ((size_t)isfe_a * S.nf + base_ck) * ncell;
             const size_t kc = (size_t)i0 * nz + j;  // this thread's first cell
@@ -611,6 +616,10 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
                 }
             }
             cl.sync();
+        }
+        if (++ph == sfe) {
+            ph = 0;
+            blk++;
         }
     }
     // the shared accumulators (written by this thread only) go to the shot's buffer
