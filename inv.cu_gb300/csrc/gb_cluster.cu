@@ -231,7 +231,6 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
     // the thread owning columns 0, 1 sends them left; the one owning columns
     // cp-2, cp-1 sends them right (a CTA with a right neighbour holds cp columns)
     const bool edge_l = rank > 0 && grp == 0, edge_r = rank < R - 1 && cb + QM == cp;
-    const int nrq = __popc(rmask);
 
     // Steps are counted as it = blk * sfe + ph (sfe > 0), kept by increments
     // instead of an integer division per step. Checkpoint index written after
@@ -257,10 +256,14 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
 #pragma unroll
             for (int f = 0; f < NV; f++) cp_async4(sbuf + f, inj_of(f) + (size_t)S.src_trace * nt + step);
         }
+        // adjoint sources: entry e by thread e (not by the entry's owner, whose
+        // row may own every surface receiver of its columns); the issuing
+        // threads wait for their copies before the barrier that precedes the
+        // owners' reads
         if (ADJ) {
+            const int ncr = min(*(volatile int *)&s_count, g.nrec_cta);
 #pragma unroll 1
-            for (int n = 0; n < nrq; n++) {
-                const int e = rbase + n;
+            for (int e = t; e < ncr; e += blockDim.x) {
                 const size_t ks = (size_t)rtab[e] * nt + step;
 #pragma unroll
                 for (int f = 0; f < NV; f++) cp_async4(rbuf + e * NV + f, inj_of(f) + ks);
@@ -290,6 +293,10 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
     cl.sync();
     if (ckpt_at(0, 0) >= 0) store_ckpt(ckpt_at(0, 0), FU, 0);  // displacement before step 0
     prefetch(0);
+    if (ADJ) {
+        cp_async_wait_all();
+        __syncthreads();
+    }
 
     unsigned rb = (unsigned)rbase, sq = (unsigned)srcq, qn = (unsigned)nq;
     unsigned fl = (edge_l ? 1u : 0u) | (edge_r ? 2u : 0u) | (zS ? 4u : 0u) | (zV ? 8u : 0u) | (grp > 0 ? 16u : 0u) |
@@ -400,9 +407,11 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
         // of velocity (after this step's update) and displacement (before the
         // next step; phase B changes neither), the next step's injection.
         if (!ADJ) {
+            // recorded samples: entry e by thread e (written by the owners in
+            // phase A, before the barrier above)
+            const int ncr = min(*(volatile int *)&s_count, g.nrec_cta);
 #pragma unroll 1
-            for (int n = 0; n < nrq; n++) {
-                const int e = rbase + n;
+            for (int e = t; e < ncr; e += blockDim.x) {
                 const size_t kr = (size_t)rtab[e] * nt + it;
                 if (PSV) {
                     S.out_x[kr] = rbuf[e * NV];
@@ -472,6 +481,7 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
                 }
             }
         }
+        if (ADJ) cp_async_wait_all();  // this thread's copies of the next step's adjoint sources
         cl.sync();
         // ---- adjoint with snap: the adjoint state of the owned grid cells at
         // each accumulation step, [slot][step][u fields, v fields][cell], for
