@@ -300,7 +300,7 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
 
     unsigned rb = (unsigned)rbase, sq = (unsigned)srcq, qn = (unsigned)nq;
     unsigned fl = (edge_l ? 1u : 0u) | (edge_r ? 2u : 0u) | (zS ? 4u : 0u) | (zV ? 8u : 0u) | (grp > 0 ? 16u : 0u) |
-                  (grp < G - 1 ? 32u : 0u) | (S.record_u ? 64u : 0u);
+                  (grp < G - 1 ? 32u : 0u) | (S.record_u ? 64u : 0u) | ((ADJ && !snap) ? 128u : 0u);
     unsigned spm = spmask;
     int ph = 0, blk = 0;  // it = blk * sfe + ph
     for (int it = 0; it < nt; it++) {
@@ -373,12 +373,13 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
                     *pu = un[f];
                 }
                 // ghosts: the left neighbour reads columns 0, 1, the right one column cp-1
+                // (displacement too for an in-pass kernel accumulation)
                 if (q < 2 && eL) {
                     const uint32_t a = lf + 4u * (uint32_t)(cp + q + 2);
 #pragma unroll
                     for (int f = 0; f < NV; f++) {
                         cl_st(a + 4u * (uint32_t)((FV + f) * fs), vn[f]);
-                        if (ADJ) cl_st(a + 4u * (uint32_t)((FU + f) * fs), un[f]);
+                        if (ADJ && (fl & 128u)) cl_st(a + 4u * (uint32_t)((FU + f) * fs), un[f]);
                     }
                 }
                 if (q == QM - 1 && eR) {
@@ -386,7 +387,7 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
 #pragma unroll
                     for (int f = 0; f < NV; f++) {
                         cl_st(a + 4u * (uint32_t)((FV + f) * fs), vn[f]);
-                        if (ADJ) cl_st(a + 4u * (uint32_t)((FU + f) * fs), un[f]);
+                        if (ADJ && (fl & 128u)) cl_st(a + 4u * (uint32_t)((FU + f) * fs), un[f]);
                     }
                 }
                 if (!ADJ && e >= 0) {
