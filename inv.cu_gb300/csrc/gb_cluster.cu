@@ -155,9 +155,9 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
     // rtab[rbase ...] in column order
     float *s_ax = sm + NF * fs;                          // ax of columns -2 .. cp+1
     int *rtab = reinterpret_cast<int *>(s_ax + cp + 4);  // g.nrec_cta entries
-    // per receiver entry NV values: the samples recorded in phase A (forward)
-    // or the next step's adjoint source (adjoint); then NV values of the next
-    // step's forward source
+    // per receiver entry NV values: the next step's adjoint source (adjoint)
+    // or, as an int, the receiver cell's field-0 offset in shared memory
+    // (forward); then NV values of the next step's forward source
     float *rbuf = reinterpret_cast<float *>(rtab + g.nrec_cta);
     float *sbuf = rbuf + (size_t)g.nrec_cta * NV;
     // adjoint with g.stage: the checkpoint the next kernel accumulation reads,
@@ -192,12 +192,18 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
         int n = 0;
 #pragma unroll
         for (int q = 0; q < QM; q++)
-            if ((rmask >> q) & 1) rtab[rbase + n++] = map[(cb + q) * nz + j];
+            if ((rmask >> q) & 1) {
+                rtab[rbase + n] = map[(cb + q) * nz + j];
+                // forward: the cell's field-0 offset in shared memory, from
+                // which the thread that writes the sample out reads it
+                if (!ADJ) reinterpret_cast<int *>(rbuf)[rbase + n] = (j + 2 + sig0 + grp * dsh) * rs + cb + q + 2;
+                n++;
+            }
     }
     int srcq = -1;  // owned column of the forward source
     if (!ADJ && S.src_trace >= 0 && S.src_j == j && S.src_i - i0 >= 0 && S.src_i - i0 < nq) srcq = S.src_i - i0;
-    // cells that inject or record
-    const unsigned spmask = rmask | (srcq >= 0 ? 1u << srcq : 0u);
+    // cells that inject (adjoint sources at receivers, the forward source)
+    const unsigned spmask = (ADJ ? rmask : 0u) | (srcq >= 0 ? 1u << srcq : 0u);
     __syncthreads();
     for (int e = t; e < NF * fs; e += blockDim.x) sm[e] = 0.f;
     if (ADJ && g.kacc)
@@ -390,10 +396,6 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
                         if (ADJ && (fl & 128u)) cl_st(a + 4u * (uint32_t)((FU + f) * fs), un[f]);
                     }
                 }
-                if (!ADJ && e >= 0) {
-#pragma unroll
-                    for (int f = 0; f < NV; f++) rbuf[e * NV + f] = (fl & 64u) ? un[f] : vn[f];
-                }
 #pragma unroll
                 for (int w = 0; w < NWA; w++) {
                     wa[w][0] = wa[w][1];
@@ -408,17 +410,21 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
         // of velocity (after this step's update) and displacement (before the
         // next step; phase B changes neither), the next step's injection.
         if (!ADJ) {
-            // recorded samples: entry e by thread e (written by the owners in
-            // phase A, before the barrier above)
+            // recorded samples, u when record_u else v (solver/fdm.h:181-196):
+            // entry e by thread e, read from the cell's place in shared memory
+            // (updated in phase A, before the barrier above; phase B leaves it)
             const int ncr = min(*(volatile int *)&s_count, g.nrec_cta);
+            const int *roff = reinterpret_cast<const int *>(rbuf);
+            const int fo = ((fl & 64u) ? FU : FV) * fs;
 #pragma unroll 1
             for (int e = t; e < ncr; e += blockDim.x) {
                 const size_t kr = (size_t)rtab[e] * nt + it;
+                const float *pc = sm + roff[e] + fo;
                 if (PSV) {
-                    S.out_x[kr] = rbuf[e * NV];
-                    S.out_z[kr] = rbuf[e * NV + NV - 1];
+                    S.out_x[kr] = pc[0];
+                    S.out_z[kr] = pc[(NV - 1) * fs];
                 } else {
-                    S.out_y[kr] = rbuf[e * NV];
+                    S.out_y[kr] = pc[0];
                 }
             }
             const int isfe = ckpt_at(ph, blk);
