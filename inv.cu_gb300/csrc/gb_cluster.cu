@@ -202,8 +202,8 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
     }
     int srcq = -1;  // owned column of the forward source
     if (!ADJ && S.src_trace >= 0 && S.src_j == j && S.src_i - i0 >= 0 && S.src_i - i0 < nq) srcq = S.src_i - i0;
-    // cells that inject (adjoint sources at receivers, the forward source)
-    const unsigned spmask = (ADJ ? rmask : 0u) | (srcq >= 0 ? 1u << srcq : 0u);
+    // the forward source's cell (adjoint sources: see the warp flag below)
+    const unsigned spmask = srcq >= 0 ? 1u << srcq : 0u;
     __syncthreads();
     for (int e = t; e < NF * fs; e += blockDim.x) sm[e] = 0.f;
     if (ADJ && g.kacc)
@@ -306,7 +306,8 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
 
     unsigned rb = (unsigned)rbase, sq = (unsigned)srcq, qn = (unsigned)nq;
     unsigned fl = (edge_l ? 1u : 0u) | (edge_r ? 2u : 0u) | (zS ? 4u : 0u) | (zV ? 8u : 0u) | (grp > 0 ? 16u : 0u) |
-                  (grp < G - 1 ? 32u : 0u) | (S.record_u ? 64u : 0u) | ((ADJ && !snap) ? 128u : 0u);
+                  (grp < G - 1 ? 32u : 0u) | (S.record_u ? 64u : 0u) | ((ADJ && !snap) ? 128u : 0u) |
+                  (__any_sync(__activemask(), rmask != 0u) ? 256u : 0u);
     unsigned spm = spmask;
     int ph = 0, blk = 0;  // it = blk * sfe + ph
     for (int it = 0; it < nt; it++) {
@@ -356,16 +357,21 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
                     const float dsy = xS ? ax_ : 0.f;
                     ds[0] = zs ? dsy + bz_ : dsy;
                 }
-                int e = -1;  // receiver entry of this cell
-                if ((spm >> q) & 1) {
-                    if ((rmask >> q) & 1) e = rbase + __popc(rmask & ((1u << q) - 1u));
-                    if (!ADJ && q == srcq) {
+                // forward source: a branch around its one cell
+                if (!ADJ && ((spm >> q) & 1) && q == srcq) {
 #pragma unroll
-                        for (int f = 0; f < NV; f++) ds[f] += sbuf[f];
-                    }
-                    if (ADJ && e >= 0) {
+                    for (int f = 0; f < NV; f++) ds[f] += sbuf[f];
+                }
+                // adjoint sources: in a warp that holds receivers (a uniform
+                // branch) every lane reads its entry (entry 0 where it has
+                // none: in bounds) and keeps the sum where the cell is one
+                if (ADJ && (fl & 256u)) {
+                    const bool hit = (rmask >> q) & 1;
+                    const int e = rbase + __popc(rmask & ((1u << q) - 1u));
 #pragma unroll
-                        for (int f = 0; f < NV; f++) ds[f] += rbuf[e * NV + f];
+                    for (int f = 0; f < NV; f++) {
+                        const float a = rbuf[e * NV + f];
+                        ds[f] = hit ? ds[f] + a : ds[f];
                     }
                 }
                 const float ab = s_ax[cb + q + 2] * azj;
