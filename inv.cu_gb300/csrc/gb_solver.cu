@@ -224,8 +224,14 @@ int Solver::init(const Config &cfg, int nx_, int nz_, float xmax_, float zmax_) 
             return GB_ERR_ARG;
         }
 
-    GB_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    {
+        int least = 0, greatest = 0;
+        GB_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        GB_CUDA_TRY(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, greatest));
+        GB_CUDA_TRY(cudaStreamCreateWithPriority(&st_side, cudaStreamNonBlocking, least));
+    }
     for (cudaEvent_t *e : {&ev_pass0, &ev_pass1, &ev_win0, &ev_win1}) GB_CUDA_TRY(cudaEventCreate(e));
+    for (cudaEvent_t *e : {&ev_round, &ev_side}) GB_CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
 
     const size_t n = ncell();
     {
@@ -310,8 +316,10 @@ void Solver::release() {
     cudaFree(d_rec_cells);
     cudaFree(kpart);
     cudaFree(snapbuf);
-    for (cudaEvent_t e : {ev_pass0, ev_pass1, ev_win0, ev_win1, ev_t0, ev_t1})
+    for (cudaEvent_t e : {ev_pass0, ev_pass1, ev_win0, ev_win1, ev_t0, ev_t1, ev_round, ev_side})
         if (e) cudaEventDestroy(e);
+    if (st_side) cudaStreamDestroy(st_side);
+    st_side = nullptr;
     if (st) cudaStreamDestroy(st);
     st = nullptr;
 }
@@ -1022,10 +1030,26 @@ int Solver::run_cluster_pass(int kind, int n) {
         g.c24x = 1.f / (24.f * dx);
         g.c9z = 9.f / (8.f * dz);
         g.c24z = 1.f / (24.f * dz);
-        GB_CUDA_TRY(launch_cluster(wp, adjp, d_slots[kind], n, g, nz, adjp ? kpart : nullptr, snap, st));
-        stats.launches += 1;
         if (snap) {
-            GB_CUDA_TRY(launch_snap_interaction(wp, d_slots[kind], n, snap, g, kpart, st));
+            // one launch per round of resident clusters; the kernel
+            // accumulation of a finished round runs on the side stream, on
+            // the SMs that the next round's clusters leave free (C2: 96 of
+            // 152 in use), so only the last round's waits for it
+            const int occ = std::max(1, cluster_occupancy(wp, g, nz));
+            const size_t snap_slot = (size_t)nsfe * (wp ? 4 : 2) * nc;
+            for (int b0 = 0; b0 < n; b0 += occ) {
+                const int nb = std::min(occ, n - b0);
+                float *sp = snap + (size_t)b0 * snap_slot, *kp = kpart + (size_t)b0 * 3 * nc;
+                GB_CUDA_TRY(launch_cluster(wp, adjp, d_slots[kind] + b0, nb, g, nz, kp, sp, st));
+                GB_CUDA_TRY(cudaEventRecord(ev_round, st));
+                GB_CUDA_TRY(cudaStreamWaitEvent(st_side, ev_round, 0));
+                GB_CUDA_TRY(launch_snap_interaction(wp, d_slots[kind] + b0, nb, sp, g, kp, st_side));
+                stats.launches += 2;
+            }
+            GB_CUDA_TRY(cudaEventRecord(ev_side, st_side));
+            GB_CUDA_TRY(cudaStreamWaitEvent(st, ev_side, 0));
+        } else {
+            GB_CUDA_TRY(launch_cluster(wp, adjp, d_slots[kind], n, g, nz, adjp ? kpart : nullptr, nullptr, st));
             stats.launches += 1;
         }
         if (adjp) {

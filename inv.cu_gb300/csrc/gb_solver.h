@@ -108,6 +108,10 @@ struct Solver {
     // graphs, keyed by (pass kind, nslots)
     std::map<std::pair<int, int>, GraphInfo> graphs;
     cudaStream_t st = nullptr;
+    // lower-priority stream for work that can fill SMs the main stream's
+    // clusters leave free (the kernel accumulation of a finished round)
+    cudaStream_t st_side = nullptr;
+    cudaEvent_t ev_round = nullptr, ev_side = nullptr;
     cudaEvent_t ev_pass0 = nullptr, ev_pass1 = nullptr, ev_win0 = nullptr, ev_win1 = nullptr;
     cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr;  // gb_solver_timer
     int win_steps = 0;
