@@ -17,8 +17,11 @@ It restates the reference algorithm:
       - envelope misfit ........... misfit/envelope.h:4-90 (Hilbert mask quirks)
 
 Pinning: the forward SH path is pinned against the reference's golden
-seismograms (example/checker/traces/*.su, see tests/golden/). Everything else
-follows the cited lines and is cross-checked by property tests.
+seismograms (example/checker/traces/*.su, see tests/golden/). On a GPU, the
+reference's own kernels (compiled from its sources into _ref/inv_ref.cubin)
+run under ref_harness.cu's restatement of its host loops (the ``ref_*``
+functions below): forward P-SV/SH, adjoint kernels, absorbing boundary and
+Gaussian filter as the reference computes them.
 """
 from __future__ import annotations
 
@@ -45,9 +48,17 @@ class OrcParams(ctypes.Structure):
     ]
 
 
+REF_SRC = os.environ.get("GBFWI_REF_SRC", "/root/reference")
+REF_CUBIN = os.path.join(_HERE, "_ref", "inv_ref.cubin")
+_REF = None
+
+
 def build() -> str:
-    """Compile the C oracle with its Makefile (gcc, no CUDA)."""
-    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    """Compile the C oracle (gcc) and the reference-kernel harness (nvcc) with
+    the Makefile, and the reference's kernels where its sources are present."""
+    subprocess.run(["make", "-s", "-C", _HERE, "all", "harness"], check=True)
+    if os.path.exists(os.path.join(REF_SRC, "inv.cu")):
+        subprocess.run(["make", "-s", "-C", _HERE, "ref", "REFSRC=" + REF_SRC], check=True)
     return os.path.join(_HERE, "_build", "liboracle.so")
 
 
@@ -499,3 +510,80 @@ def problem_from_config(cfg: Config, model: str = "model_true") -> Problem:
                    rec_id=(calc_idx(rec[:, 0], xmax, nx), calc_idx(rec[:, 1], zmax, nz)),
                    inv_lambda=bool(cfg.iv("inv_lambda")), inv_mu=bool(cfg.iv("inv_mu")),
                    inv_rho=bool(cfg.iv("inv_rho")))
+
+
+# ----------------------------------------------------------------------------
+# The reference's own kernels (ref_harness.cu; needs a GPU and _ref/inv_ref.cubin)
+# ----------------------------------------------------------------------------
+def ref_available() -> bool:
+    return os.path.exists(REF_CUBIN) and os.path.exists(os.path.join(_HERE, "_build", "libref_harness.so"))
+
+
+def ref_lib():
+    """The harness, with the reference's cubin loaded (raises when absent)."""
+    global _REF
+    if _REF is None:
+        lib_ = ctypes.CDLL(os.path.join(_HERE, "_build", "libref_harness.so"))
+        lib_.ref_last_error.restype = ctypes.c_char_p
+        if lib_.ref_open(REF_CUBIN.encode()) != 0:
+            raise RuntimeError("reference kernels: " + lib_.ref_last_error().decode())
+        _REF = lib_
+    return _REF
+
+
+def _ref_check(rc, what):
+    if rc != 0:
+        raise RuntimeError("%s: %s" % (what, ref_lib().ref_last_error().decode()))
+
+
+def ref_absbound(nx, nz, width, alpha, left, right, bottom, top) -> np.ndarray:
+    """initAbsbound (solver/fdm.h:48-74) run by the reference's kernel."""
+    out = np.zeros(nx * nz, np.float32)
+    _ref_check(ref_lib().ref_absbound(nx, nz, int(width), ctypes.c_float(alpha), int(left), int(right),
+                                      int(bottom), int(top), _p(out)), "ref_absbound")
+    return out
+
+
+def ref_forward(pb: Problem, isrc: int, adj: bool = True, record_u: bool | None = None, ab=None):
+    """FdmSolver::runForward with the reference's kernels; as forward() (one
+    wave system). ab: absorbing profile (default pb.ab)."""
+    if record_u is None:
+        record_u = adj
+    n = pb.nx * pb.nz
+    outs = [np.zeros(pb.nrec * pb.nt, np.float32) for _ in range(3)]
+    nsfe = pb.nt // pb.sfe if (adj and pb.sfe) else 0
+    ckpt = np.zeros(nsfe * pb.nckpt() * n, np.float32) if nsfe else None
+    mats = [_cast(a, np.float32) for a in (pb.lam, pb.mu, pb.rho, pb.ab if ab is None else ab)]
+    stf = [_cast(a, np.float32) for a in pb.stf]
+    ids = [_cast(a, np.int32) for a in (*pb.src_id, *pb.rec_id)]
+    prm = pb.params(adj, record_u)
+    _ref_check(ref_lib().ref_forward(ctypes.byref(prm), *[_p(a) for a in mats], *[_p(a) for a in stf],
+                                     *[_p(a) for a in ids], ctypes.c_int(isrc), *[_p(o) for o in outs], _p(ckpt)),
+               "ref_forward")
+    outs = [o.reshape(pb.nrec, pb.nt) for o in outs]
+    if ckpt is not None:
+        ckpt = ckpt.reshape(nsfe, pb.nckpt(), n)
+    return outs[0], outs[1], outs[2], ckpt
+
+
+def ref_adjoint(pb: Problem, adstf, ckpt, kernels=None, ab=None):
+    """FdmSolver::runAdjoint with the reference's kernels; as adjoint()."""
+    n = pb.nx * pb.nz
+    if kernels is None:
+        kernels = [np.zeros(n, np.float32) for _ in range(3)]
+    kernels = [_cast(k, np.float32).copy() for k in kernels]
+    mats = [_cast(a, np.float32) for a in (pb.lam, pb.mu, pb.rho, pb.ab if ab is None else ab)]
+    ad = [_cast(a, np.float32).ravel() for a in adstf]
+    ids = [_cast(a, np.int32) for a in pb.rec_id]
+    ck = _cast(ckpt, np.float32).ravel()
+    prm = pb.params(True, True)
+    _ref_check(ref_lib().ref_adjoint(ctypes.byref(prm), *[_p(a) for a in mats], *[_p(a) for a in ad],
+                                     *[_p(a) for a in ids], _p(ck), *[_p(k) for k in kernels]), "ref_adjoint")
+    return kernels
+
+
+def ref_gaussian(nx, nz, sigma, data) -> np.ndarray:
+    """GaussianFilter::init + apply (filter/gaussian.h:37-61) with the reference's kernels."""
+    d = np.ascontiguousarray(data, np.float32).copy()
+    _ref_check(ref_lib().ref_gaussian(nx, nz, int(sigma), _p(d)), "ref_gaussian")
+    return d
