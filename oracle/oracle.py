@@ -587,3 +587,17 @@ def ref_gaussian(nx, nz, sigma, data) -> np.ndarray:
     d = np.ascontiguousarray(data, np.float32).copy()
     _ref_check(ref_lib().ref_gaussian(nx, nz, int(sigma), _p(d)), "ref_gaussian")
     return d
+
+
+def ref_misfit(kind: int, syn, obs, dt: float):
+    """The reference's per-trace misfit (misfit/waveform.h, misfit/envelope.h)
+    with its kernels, cuFFT and cuBLAS: syn/obs [ntr, nt] -> (values [ntr],
+    adstf [ntr, nt])."""
+    syn = _cast(syn, np.float32)
+    obs = _cast(obs, np.float32)
+    ntr, nt = syn.shape
+    ad = np.zeros((ntr, nt), np.float32)
+    val = np.zeros(ntr, np.float32)
+    _ref_check(ref_lib().ref_misfit(int(kind), int(ntr), int(nt), ctypes.c_double(dt), _p(syn), _p(obs), _p(ad),
+                                    _p(val)), "ref_misfit")
+    return val, ad

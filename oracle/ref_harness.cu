@@ -14,13 +14,20 @@
 //   divS / divV            solver/fdm.h:273-294
 //   initAbsbound           solver/fdm.h:48-74 (launched as in fdm.h:453-456)
 //   GaussianFilter         filter/gaussian.h:37-61
+//   WaveformMisfit::run    misfit/waveform.h:35-40 (taper: waveform.h:44-51)
+//   EnvelopeMisfit::run    misfit/envelope.h:58-90 (hilbert: envelope.h:91-98)
+// (the misfits with cuFFT and cuBLAS as the reference calls them, one trace
+// at a time, device::amax/norm from lib/device.h:170-180)
 // with the reference's launch shapes (Dim::init, lib/device.h:46-57, with
 // device::nthread = 0: nx blocks of nz threads).
 //
 // Checkpoint layout (the C oracle's): ckpt[(isfe * nf + q) * n], q over
 // (uy, vy) for SH or (ux, uz, vx, vz) for P-SV; one wave system per call.
+#include <cublas_v2.h>
 #include <cuda_runtime.h>
+#include <cufft.h>
 
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -45,7 +52,8 @@ Dim make_dim(int nx, int nz) { return Dim{nx, nz, nx, nz, nx * nz}; }
 
 enum K {
     K_DIVSY, K_DIVSXZ, K_DIVVY, K_DIVVXZ, K_UPDSY, K_UPDSXZ, K_UPDVY, K_UPDVXZ, K_ADDSTF, K_SAVEREC,
-    K_IRHOY, K_IRHOXZ, K_IMUY, K_IMUXZ, K_ILAMXZ, K_ABS, K_GINIT, K_GX, K_GZ, K_N
+    K_IRHOY, K_IRHOXZ, K_IMUY, K_IMUXZ, K_ILAMXZ, K_ABS, K_GINIT, K_GX, K_GZ,
+    K_TAPER, K_DIFF, K_HILB, K_R2C, K_C2IMAG, K_C2ABS, K_ETMP, K_ESTF, K_MUL, K_AXPBY, K_N
 };
 // names as nvcc reports them for the reference's kernels
 const char *kNames[K_N] = {
@@ -68,6 +76,16 @@ const char *kNames[K_N] = {
     "_ZN15_GaussianFilter18initialiseGaussianEPfm3Dim",
     "_ZN15_GaussianFilter13filterKernelXEPfS0_m3Dim",
     "_ZN15_GaussianFilter13filterKernelZEPfS0_S0_m3Dim",
+    "_ZN15_WaveformMisfit5taperEPffi",
+    "_ZN15_WaveformMisfit4diffEPfS0_S0_S0_S0_m",
+    "_ZN15_EnvelopeMisfit8_hilbertEP6float2m",
+    "_ZN15_EnvelopeMisfit7copyR2CEP6float2Pf",
+    "_ZN15_EnvelopeMisfit10copyC2ImagEPfP6float2i",
+    "_ZN15_EnvelopeMisfit9copyC2AbsEPfP6float2i",
+    "_ZN15_EnvelopeMisfit11envelopeTmpEPfS0_S0_f",
+    "_ZN15_EnvelopeMisfit18prepareEnvelopeSTFEPfS0_S0_S0_m",
+    "_ZN6device5_calcEPfS0_S0_3Dim",
+    "_ZN6device5_calcEPffS0_fS0_3Dim",
 };
 
 cudaLibrary_t g_lib = nullptr;
@@ -368,6 +386,104 @@ int ref_gaussian(int nx, int nz, int sigma, float *data) {
         return 1;
     REF_TRY(cudaDeviceSynchronize());
     return to_host(data, d, n);
+}
+
+// Misfit::run's per-trace misfit (misfit/misfit.h:29-41) for ntr traces of
+// nt samples: type 0 waveform, 1 envelope. Writes each trace's adjoint source
+// (adstf [ntr*nt]) and value (values [ntr], as the reference returns it).
+int ref_misfit(int type, int ntr, int nt, double dt_in, const float *syn, const float *obs, float *adstf,
+               float *values) {
+    if (!g_lib || ntr < 1 || nt < 2 || (type != 0 && type != 1)) return 1;
+    const size_t n = (size_t)ntr * nt;
+    Bufs b;
+    float *ds = b.alloc<float>(n), *dob = b.alloc<float>(n), *dad = b.alloc<float>(n);
+    float *misfit = b.alloc<float>(nt), *tw = b.alloc<float>(nt);
+    float *esyn = b.alloc<float>(nt), *eobs = b.alloc<float>(nt), *ersd = b.alloc<float>(nt),
+          *etmp = b.alloc<float>(nt);
+    float2 *csyn = b.alloc<float2>(nt), *cobs = b.alloc<float2>(nt);
+    if (!ds || !dob || !dad || !misfit || !tw || !esyn || !eobs || !ersd || !etmp || !csyn || !cobs) return 1;
+    if (to_dev(ds, syn, n) || to_dev(dob, obs, n)) return 1;
+    cublasHandle_t cb = nullptr;
+    if (cublasCreate(&cb) != CUBLAS_STATUS_SUCCESS) {
+        g_err = "cublasCreate";
+        return 1;
+    }
+    cufftHandle plan = 0;
+    if (type == 1 && cufftPlan1d(&plan, nt, CUFFT_C2C, 1) != CUFFT_SUCCESS) {
+        cublasDestroy(cb);
+        g_err = "cufftPlan1d";
+        return 1;
+    }
+    const float dt = (float)dt_in;
+    size_t ntv = (size_t)nt;
+    int nti = nt;
+    Dim dim = make_dim(nt, 1);  // Dim(nt, 1): nt blocks of one thread
+    int rc = 0;
+    auto hilbert = [&](float *x, float2 *data) -> int {
+        void *a0[] = {&data, &x};
+        void *a1[] = {&data, &ntv};
+        if (launch(K_R2C, nt, 1, a0)) return 1;
+        if (cufftExecC2C(plan, data, data, CUFFT_FORWARD) != CUFFT_SUCCESS) return 1;
+        if (launch(K_HILB, nt, 1, a1)) return 1;
+        return cufftExecC2C(plan, data, data, CUFFT_INVERSE) != CUFFT_SUCCESS;
+    };
+    if (type == 0) {
+        void *a[] = {&tw, (void *)&dt, &nti};
+        rc = launch(K_TAPER, nt, 1, a);
+    }
+    for (int r = 0; r < ntr && !rc; r++) {
+        float *sy = ds + (size_t)r * nt, *ob = dob + (size_t)r * nt, *ad = dad + (size_t)r * nt;
+        float v = 0.f;
+        if (type == 0) {
+            void *a[] = {&sy, &ob, &ad, &misfit, &tw, &ntv};
+            if (launch(K_DIFF, nt, 1, a) || cublasSnrm2(cb, nt, misfit, 1, &v) != CUBLAS_STATUS_SUCCESS) {
+                rc = 1;
+                break;
+            }
+        } else {
+            if (hilbert(sy, csyn) || hilbert(ob, cobs)) {
+                rc = 1;
+                break;
+            }
+            void *a0[] = {&esyn, &csyn, &nti};
+            void *a1[] = {&eobs, &cobs, &nti};
+            if (launch(K_C2ABS, nt, 1, a0) || launch(K_C2ABS, nt, 1, a1)) {
+                rc = 1;
+                break;
+            }
+            int idx = 0;
+            float e = 0.f;
+            if (cublasIsamax(cb, nt, esyn, 1, &idx) != CUBLAS_STATUS_SUCCESS ||
+                cudaMemcpy(&e, esyn + idx - 1, 4, cudaMemcpyDeviceToHost) != cudaSuccess) {
+                rc = 1;
+                break;
+            }
+            float mx = std::fabs(e) * 0.05;  // device::amax(...) * 0.05 into a float
+            if (mx < 0.05) mx = 0.05;
+            void *a2[] = {&etmp, &esyn, &eobs, &mx};
+            void *a3[] = {&ersd, &csyn, &nti};
+            void *a4[] = {&ersd, &ersd, &etmp, &dim};
+            void *a5[] = {&ersd, &cobs, &nti};
+            void *a6[] = {&ad, &etmp, &sy, &ersd, &ntv};
+            float one = 1.f, mone = -1.f;
+            void *a7[] = {&ersd, &one, &esyn, &mone, &eobs, &dim};
+            if (launch(K_ETMP, nt, 1, a2) || launch(K_C2IMAG, nt, 1, a3) || launch(K_MUL, dim.dg, dim.db, a4) ||
+                hilbert(ersd, cobs) || launch(K_C2IMAG, nt, 1, a5) || launch(K_ESTF, nt, 1, a6) ||
+                launch(K_AXPBY, dim.dg, dim.db, a7) || cublasSnrm2(cb, nt, ersd, 1, &v) != CUBLAS_STATUS_SUCCESS) {
+                rc = 1;
+                break;
+            }
+        }
+        values[r] = v * std::sqrt(dt);
+    }
+    if (plan) cufftDestroy(plan);
+    cublasDestroy(cb);
+    if (rc) {
+        if (g_err.empty()) g_err = "ref_misfit";
+        return 1;
+    }
+    REF_TRY(cudaDeviceSynchronize());
+    return to_host(adstf, dad, n);
 }
 
 }  // extern "C"

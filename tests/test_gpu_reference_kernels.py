@@ -5,7 +5,7 @@ sources into oracle/_ref/inv_ref.cubin, run under oracle/ref_harness.cu's
 restatement of its host loops (runForward, runAdjoint, GaussianFilter). The
 GB300 path and the C oracle are compared with what they compute, on the
 same inputs: seismograms within relative L2 1e-5 after the full time loop,
-kernels within 1e-4, filter and absorbing profile within 1e-6.
+kernels and misfits within 1e-4, filter and absorbing profile within 1e-6.
 
 The reference divides where the GB300 kernels multiply by reciprocals and
 contracts its own expressions into FMAs, so results agree to rounding, not
@@ -127,3 +127,46 @@ def test_gaussian_filter_matches_reference_kernels(gpu, ref, nx, nz, sigma):
     g = gpu.GaussianFilter(nx, nz, sigma).apply_host(data)
     assert cases.rel(g, r) < 1e-6
     assert cases.rel(ref.gaussian_filter(nx, nz, sigma, data), r) < 1e-6
+
+
+@pytest.mark.parametrize("kind,wave", [(0, "sh"), (0, "psv"), (1, "sh"), (1, "psv")])
+def test_misfit_matches_reference_kernels(gpu, ref, kind, wave):
+    """Waveform (0) and envelope (1) misfits: per-trace values and adjoint
+    sources of the C oracle, and the GB300 misfit's total and adjoint
+    sources, against the reference's per-trace run (its kernels, cuFFT and
+    cuBLAS); the GB300 total is an FP64 sum of the per-trace values."""
+    case = cases.make_case(wave=wave, nx=100, nz=80, nt=512 if kind else 400, nsrc=2, nrec=24, seed=31)
+    cfg, sol = cases.gpu_solver(gpu, case)
+    pb = cases.oracle_problem(ref, case)
+    pert = dict(case)
+    pert["vs"] = (case["vs"] * 1.03).astype(np.float32)
+    pert["vp"] = (case["vp"] * 1.02).astype(np.float32)
+    pbo = cases.oracle_problem(ref, pert)
+    obs, syn = {c: [] for c in "xyz"}, {c: [] for c in "xyz"}
+    for s in range(case["nsrc"]):
+        o = ref.forward(pbo, s, adj=True)
+        y = ref.forward(pb, s, adj=True)
+        for q, c in enumerate("xyz"):
+            obs[c].append(o[q])
+            syn[c].append(y[q])
+    total = 0.0
+    last = {}
+    tw = ref.taper(case["nt"], case["dt"])
+    for s in range(case["nsrc"]):
+        for c in comps(wave):
+            v, ad = ref.ref_misfit(kind, syn[c][s], obs[c][s], case["dt"])
+            total += float(np.sum(v.astype(np.float64)))
+            for r in range(pb.nrec):
+                if kind == 0:
+                    ov, oad = ref.waveform_misfit(syn[c][s][r:r + 1], obs[c][s][r:r + 1], tw, case["dt"])
+                else:
+                    ov, oad = ref.envelope_misfit(syn[c][s][r:r + 1], obs[c][s][r:r + 1], case["dt"])
+                assert abs(ov - v[r]) <= 1e-4 * abs(v[r]) + 1e-12, (s, c, r)
+                assert cases.rel(oad[0], ad[r]) < 1e-4, (s, c, r)
+            last[c] = ad
+    m = gpu.Misfit.from_obs(kind, sol, {c: np.stack(obs[c]) for c in comps(wave)})
+    val = m.run(kernel=False)
+    assert abs(val - total) / abs(total) < 1e-4
+    slot = (case["nsrc"] - 1) % sol.capacity
+    for c in comps(wave):
+        assert cases.rel(sol.adstf(c, slot=slot), last[c]) < 1e-4, c
