@@ -149,7 +149,11 @@ int gb_solver_batch_capacity(gb_solver *s);
  * unshifted rows), "cluster_snap" (1: a cluster adjoint stores its state at
  * every accumulation step and a separate kernel accumulates the kernels
  * after the pass, when that state fits in a quarter of the free device
- * memory, default; 0: accumulates in the pass), "cluster_qm" (columns per
+ * memory, default; 0: accumulates in the pass), "pipeline" (1: a gradient
+ * whose cluster passes run in more than one round of resident clusters
+ * overlaps each round's misfit with the next forward round and the previous
+ * adjoint round, default; 0: forward, misfit and adjoint one after another),
+ * "cluster_qm" (columns per
  * thread of the cluster pass: 0 = chosen with the cluster size, or 4, 8, 10,
  * 12, 16, 20, 24), "hbm_budget_gb". Options
  * change no forward result; "ckpt" changes kernels by the checkpoint

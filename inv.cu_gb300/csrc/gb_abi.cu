@@ -317,6 +317,8 @@ int gb_solver_set_option(gb_solver *s, const char *key, double value) {
         v.opt_shift = value != 0;
     } else if (k == "cluster_snap") {
         v.opt_snap = value != 0;
+    } else if (k == "pipeline") {
+        v.opt_pipe = value != 0;
     } else if (k == "tma") {
         v.opt_tma = value != 0;
         v.invalidate_graphs();

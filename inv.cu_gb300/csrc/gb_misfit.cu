@@ -203,6 +203,10 @@ struct gb_misfit {
     float *etmp = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     long long launches = 0;
+    // pipelined batches: per-round timing events, per-trace values in pinned memory
+    std::vector<cudaEvent_t> ev_r0, ev_r1;
+    double *h_pin = nullptr;
+    size_t h_pin_n = 0;
 
     int comps(int *c) const {
         int n = 0;
@@ -235,8 +239,9 @@ static int misfit_alloc(gb_misfit *m) {
     return GB_OK;
 }
 
-static int misfit_tables(gb_misfit *m, const int *shots, int n) {
+static int misfit_tables(gb_misfit *m, const int *shots, int n, cudaStream_t st = nullptr) {
     Solver &s = *m->s;
+    if (!st) st = s.st;
     int cs[3];
     const int nc = m->comps(cs);
     const size_t ntr = (size_t)n * nc * s.nrec;
@@ -260,7 +265,7 @@ static int misfit_tables(gb_misfit *m, const int *shots, int n) {
                 m->h_tr[q].adstf = s.slots[b].adstf[c] + off;
                 q++;
             }
-    GB_CUDA_TRY(cudaMemcpyAsync(m->d_tr, m->h_tr.data(), ntr * sizeof(TraceRef), cudaMemcpyHostToDevice, s.st));
+    GB_CUDA_TRY(cudaMemcpyAsync(m->d_tr, m->h_tr.data(), ntr * sizeof(TraceRef), cudaMemcpyHostToDevice, st));
     return GB_OK;
 }
 
@@ -291,33 +296,39 @@ static int fft_error() {
     return GB_ERR_CUDA;
 }
 
-static int envelope_run(gb_misfit *m, int ntr) {
+// traces [tr0, tr0 + ntr) of the table, on stream st
+static int envelope_run(gb_misfit *m, int ntr, int tr0 = 0, cudaStream_t st = nullptr) {
     Solver &s = *m->s;
+    if (!st) st = s.st;
     const int rows = std::min(ntr, 4096);
     int rc = envelope_plans(m, rows);
     if (rc) return rc;
+    cufftSetStream(m->plan2, st);
+    cufftSetStream(m->plan1, st);
     const float sq = std::sqrt(s.dt);
-    for (int first = 0; first < ntr; first += rows) {
-        const int r = std::min(rows, ntr - first);
-        k_env_load<<<2 * r, 256, 0, s.st>>>(m->cbuf, m->d_tr, first, r, s.nt);
+    for (int first = tr0; first < tr0 + ntr; first += rows) {
+        const int r = std::min(rows, tr0 + ntr - first);
+        k_env_load<<<2 * r, 256, 0, st>>>(m->cbuf, m->d_tr, first, r, s.nt);
         GB_CUDA_TRY(cudaGetLastError());
         // rows [0, r) hold synthetics and [r, 2r) observations; a short tail
         // still runs the full plan, the rows past 2r are never read
         if (cufftExecC2C(m->plan2, m->cbuf, m->cbuf, CUFFT_FORWARD) != CUFFT_SUCCESS) return fft_error();
-        k_env_mask<<<2 * r, 256, 0, s.st>>>(m->cbuf, s.nt);
+        k_env_mask<<<2 * r, 256, 0, st>>>(m->cbuf, s.nt);
         GB_CUDA_TRY(cudaGetLastError());
         if (cufftExecC2C(m->plan2, m->cbuf, m->cbuf, CUFFT_INVERSE) != CUFFT_SUCCESS) return fft_error();
-        k_env_mid<<<r, 256, 0, s.st>>>(m->cbuf, m->etmp, r, s.nt, sq, m->d_val + first);
+        k_env_mid<<<r, 256, 0, st>>>(m->cbuf, m->etmp, r, s.nt, sq, m->d_val + first);
         GB_CUDA_TRY(cudaGetLastError());
         cufftComplex *co = m->cbuf + (size_t)r * s.nt;
         if (cufftExecC2C(m->plan1, co, co, CUFFT_FORWARD) != CUFFT_SUCCESS) return fft_error();
-        k_env_mask<<<r, 256, 0, s.st>>>(co, s.nt);
+        k_env_mask<<<r, 256, 0, st>>>(co, s.nt);
         GB_CUDA_TRY(cudaGetLastError());
         if (cufftExecC2C(m->plan1, co, co, CUFFT_INVERSE) != CUFFT_SUCCESS) return fft_error();
-        k_env_final<<<r, 256, 0, s.st>>>(m->cbuf, m->etmp, m->d_tr, first, r, s.nt);
+        k_env_final<<<r, 256, 0, st>>>(m->cbuf, m->etmp, m->d_tr, first, r, s.nt);
         GB_CUDA_TRY(cudaGetLastError());
         m->launches += 5;
     }
+    cufftSetStream(m->plan2, s.st);
+    cufftSetStream(m->plan1, s.st);
     return GB_OK;
 }
 
@@ -355,6 +366,78 @@ static int misfit_batch(gb_misfit *m, const int *shots, int n) {
     return GB_OK;
 }
 
+// Pipelined misfit of a batch whose forward pass runs as rounds (the
+// solver's pipe_plan): round r's traces are processed on the side stream as
+// soon as that round's forward has finished, overlapping the next round on
+// the SMs its clusters leave free, and each round signals the adjoint round
+// that needs it. Per-trace values land in pinned memory; misfit_pipe_finish
+// books them once the adjoint pass has synchronised.
+static int misfit_batch_pipe(gb_misfit *m, const int *shots, int n) {
+    Solver &s = *m->s;
+    int cs[3];
+    const int nc = m->comps(cs);
+    const int per_shot = nc * s.nrec;
+    const int ntr = n * per_shot;
+    if (ntr == 0) return GB_OK;
+    // the trace table of the batch, uploaded on the side stream ahead of its
+    // first wait (the main stream is still running the forward rounds)
+    int rc = misfit_tables(m, shots, n, s.st_side);
+    if (rc) return rc;
+    if (m->h_pin_n < (size_t)ntr) {
+        if (m->h_pin) cudaFreeHost(m->h_pin);
+        m->h_pin = nullptr;
+        m->h_pin_n = 0;
+        GB_CUDA_TRY(cudaMallocHost(&m->h_pin, (size_t)ntr * sizeof(double)));
+        m->h_pin_n = ntr;
+    }
+    while ((int)m->ev_r0.size() < s.pipe_rounds) {
+        cudaEvent_t a = nullptr, b = nullptr;
+        GB_CUDA_TRY(cudaEventCreate(&a));
+        GB_CUDA_TRY(cudaEventCreate(&b));
+        m->ev_r0.push_back(a);
+        m->ev_r1.push_back(b);
+    }
+    cudaStream_t side = s.st_side;
+    for (int r = 0; r < s.pipe_rounds; r++) {
+        const int b0 = r * s.pipe_occ, nb = std::min(s.pipe_occ, n - b0);
+        const int tr0 = b0 * per_shot, ntr_r = nb * per_shot;
+        GB_CUDA_TRY(cudaStreamWaitEvent(side, s.ev_fwd_round[r], 0));
+        GB_CUDA_TRY(cudaEventRecord(m->ev_r0[r], side));
+        if (m->type == 0) {
+            k_waveform<<<ntr_r, 256, 0, side>>>(m->d_tr + tr0, m->tw, s.nt, std::sqrt(s.dt), m->d_val + tr0);
+            GB_CUDA_TRY(cudaGetLastError());
+            m->launches += 1;
+        } else {
+            rc = envelope_run(m, ntr_r, tr0, side);
+            if (rc) return rc;
+        }
+        GB_CUDA_TRY(cudaEventRecord(m->ev_r1[r], side));
+        GB_CUDA_TRY(cudaEventRecord(s.ev_mis_round[r], side));
+    }
+    GB_CUDA_TRY(cudaMemcpyAsync(m->h_pin, m->d_val, (size_t)ntr * sizeof(double), cudaMemcpyDeviceToHost, side));
+    return GB_OK;
+}
+
+// After the pipelined batch's adjoint (or a synchronisation of both streams):
+// per-trace values into h_val, misfit time booked.
+static int misfit_pipe_finish(gb_misfit *m, const int *shots, int n) {
+    Solver &s = *m->s;
+    GB_CUDA_TRY(cudaStreamSynchronize(s.st_side));
+    int cs[3];
+    const int per_shot = m->comps(cs) * s.nrec;
+    for (int r = 0; r < s.pipe_rounds; r++) {
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, m->ev_r0[r], m->ev_r1[r]) == cudaSuccess)
+            s.stats.misfit_ms += ms;
+        else
+            (void)cudaGetLastError();
+    }
+    for (int b = 0; b < n; b++)
+        std::copy(m->h_pin + (size_t)b * per_shot, m->h_pin + (size_t)(b + 1) * per_shot,
+                  m->h_val.begin() + (size_t)shots[b] * per_shot);
+    return GB_OK;
+}
+
 static int misfit_run(gb_misfit *m, bool kernel, bool snapshot, double *value) {
     Solver &s = *m->s;
     if (kernel) {
@@ -369,6 +452,23 @@ static int misfit_run(gb_misfit *m, bool kernel, bool snapshot, double *value) {
         shots.clear();
         for (int is = first; is < std::min(s.nsrc, first + bsz); is++) shots.push_back(is);
         const int n = (int)shots.size();
+        // a gradient whose forward runs in rounds of resident clusters: the
+        // misfit of each round overlaps the next round of the forward and the
+        // adjoint of the previous one
+        if (kernel && !snapshot && s.pipe_plan(shots.data(), n) > 1) {
+            s.pipe_on = true;
+            rc = s.forward(shots.data(), n, true, true, false);
+            if (!rc) rc = misfit_batch_pipe(m, shots.data(), n);
+            if (!rc) rc = s.adjoint(shots.data(), n, false, shots[0]);
+            s.pipe_on = false;
+            if (!rc) rc = misfit_pipe_finish(m, shots.data(), n);
+            if (rc) {
+                cudaStreamSynchronize(s.st_side);
+                (void)s.book_forward_pass();
+                return rc;
+            }
+            continue;
+        }
         rc = s.forward(shots.data(), n, kernel, s.adj || s.trace_type == 1, false);
         if (rc) return rc;
         rc = misfit_batch(m, shots.data(), n);
@@ -547,6 +647,9 @@ void gb_misfit_destroy(gb_misfit *m) {
     if (m->e0) cudaEventDestroy(m->e0);
     if (m->e1) cudaEventDestroy(m->e1);
     if (m->own_filter) gb_filter_destroy(m->filter);
+    for (cudaEvent_t e : m->ev_r0) cudaEventDestroy(e);
+    for (cudaEvent_t e : m->ev_r1) cudaEventDestroy(e);
+    if (m->h_pin) cudaFreeHost(m->h_pin);
     delete m;
 }
 

@@ -180,6 +180,7 @@ int Solver::init(const Config &cfg, int nx_, int nz_, float xmax_, float zmax_) 
     if (cfg.has("cluster_kacc")) opt_kacc = cfg.iv("cluster_kacc") != 0;
     if (cfg.has("cluster_shift")) opt_shift = cfg.iv("cluster_shift") != 0;
     if (cfg.has("cluster_snap")) opt_snap = cfg.iv("cluster_snap") != 0;
+    if (cfg.has("pipeline")) opt_pipe = cfg.iv("pipeline") != 0;
     if (cfg.has("cluster")) opt_cluster = std::max(0, std::min(16, cfg.iv("cluster")));
     nx = nx_;
     nz = nz_;
@@ -232,6 +233,7 @@ int Solver::init(const Config &cfg, int nx_, int nz_, float xmax_, float zmax_) 
     }
     for (cudaEvent_t *e : {&ev_pass0, &ev_pass1, &ev_win0, &ev_win1}) GB_CUDA_TRY(cudaEventCreate(e));
     for (cudaEvent_t *e : {&ev_round, &ev_side}) GB_CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    for (cudaEvent_t *e : {&ev_fpass0, &ev_fpass1}) GB_CUDA_TRY(cudaEventCreate(e));
 
     const size_t n = ncell();
     {
@@ -316,8 +318,12 @@ void Solver::release() {
     cudaFree(d_rec_cells);
     cudaFree(kpart);
     cudaFree(snapbuf);
-    for (cudaEvent_t e : {ev_pass0, ev_pass1, ev_win0, ev_win1, ev_t0, ev_t1, ev_round, ev_side})
+    for (cudaEvent_t e : {ev_pass0, ev_pass1, ev_win0, ev_win1, ev_t0, ev_t1, ev_round, ev_side, ev_fpass0, ev_fpass1})
         if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : ev_fwd_round) cudaEventDestroy(e);
+    for (cudaEvent_t e : ev_mis_round) cudaEventDestroy(e);
+    ev_fwd_round.clear();
+    ev_mis_round.clear();
     if (st_side) cudaStreamDestroy(st_side);
     st_side = nullptr;
     if (st) cudaStreamDestroy(st);
@@ -952,10 +958,11 @@ bool Solver::cluster_ok(const int *shots, int n, bool snapshot) const {
 // One pass with the cluster-resident kernel: one launch per wave system.
 int Solver::run_cluster_pass(int kind, int n) {
     const size_t nc = ncell();
-    GB_CUDA_TRY(cudaEventRecord(ev_pass0, st));
+    const bool adjp = kind == PASS_ADJ;
+    const bool pipe_fwd = pipe_on && !adjp && pipe_rounds > 1;  // returns without waiting
+    GB_CUDA_TRY(cudaEventRecord(pipe_fwd ? ev_fpass0 : ev_pass0, st));
     GB_CUDA_TRY(launch_reciprocal(rinv, rho, nc, st));
     stats.launches += 1;
-    const bool adjp = kind == PASS_ADJ;
     if (adjp) {
         if (kpart_slots < (size_t)n) {
             GB_CUDA_TRY(cudaStreamSynchronize(st));
@@ -1040,6 +1047,10 @@ int Solver::run_cluster_pass(int kind, int n) {
             for (int b0 = 0; b0 < n; b0 += occ) {
                 const int nb = std::min(occ, n - b0);
                 float *sp = snap + (size_t)b0 * snap_slot, *kp = kpart + (size_t)b0 * 3 * nc;
+                // pipelined: this round's shots need their own misfit only
+                if (pipe_on && pipe_rounds > 1)
+                    for (int r = b0 / pipe_occ; r <= (b0 + nb - 1) / pipe_occ && r < pipe_rounds; r++)
+                        GB_CUDA_TRY(cudaStreamWaitEvent(st, ev_mis_round[r], 0));
                 GB_CUDA_TRY(launch_cluster(wp, adjp, d_slots[kind] + b0, nb, g, nz, kp, sp, st));
                 GB_CUDA_TRY(cudaEventRecord(ev_round, st));
                 GB_CUDA_TRY(cudaStreamWaitEvent(st_side, ev_round, 0));
@@ -1048,7 +1059,18 @@ int Solver::run_cluster_pass(int kind, int n) {
             }
             GB_CUDA_TRY(cudaEventRecord(ev_side, st_side));
             GB_CUDA_TRY(cudaStreamWaitEvent(st, ev_side, 0));
+        } else if (pipe_fwd) {
+            // one launch per round; the caller's misfit of a round starts on
+            // the side stream once the round's event has fired
+            for (int r = 0, b0 = 0; b0 < n; r++, b0 += pipe_occ) {
+                const int nb = std::min(pipe_occ, n - b0);
+                GB_CUDA_TRY(launch_cluster(wp, false, d_slots[kind] + b0, nb, g, nz, nullptr, nullptr, st));
+                GB_CUDA_TRY(cudaEventRecord(ev_fwd_round[r], st));
+                stats.launches += 1;
+            }
         } else {
+            if (adjp && pipe_on && pipe_rounds > 1)
+                for (int r = 0; r < pipe_rounds; r++) GB_CUDA_TRY(cudaStreamWaitEvent(st, ev_mis_round[r], 0));
             GB_CUDA_TRY(launch_cluster(wp, adjp, d_slots[kind], n, g, nz, adjp ? kpart : nullptr, nullptr, st));
             stats.launches += 1;
         }
@@ -1063,6 +1085,13 @@ int Solver::run_cluster_pass(int kind, int n) {
         if (adjp) stats.cluster_adj = (g.stage ? 1 : 0) | (g.kacc ? 2 : 0) | (snap ? 4 : 0);
         stats.cluster_shift = g.dshift;
     }
+    stats.cell_updates += (long long)nc * nt * n;
+    last_par = nt & 1;
+    if (pipe_fwd) {
+        GB_CUDA_TRY(cudaEventRecord(ev_fpass1, st));
+        fpass_pending = true;
+        return GB_OK;
+    }
     GB_CUDA_TRY(cudaEventRecord(ev_pass1, st));
     GB_CUDA_TRY(cudaStreamSynchronize(st));
     float ms = 0;
@@ -1074,9 +1103,40 @@ int Solver::run_cluster_pass(int kind, int n) {
     // the whole pass is one kernel per system: book it as nt steps
     stats.step_ms += ms;
     stats.step_launches += nt;
-    stats.cell_updates += (long long)nc * nt * n;
-    last_par = nt & 1;
+    return book_forward_pass();
+}
+
+// the forward pass of a pipelined gradient, booked once it has finished
+int Solver::book_forward_pass() {
+    if (!fpass_pending) return GB_OK;
+    GB_CUDA_TRY(cudaEventSynchronize(ev_fpass1));
+    float ms = 0;
+    GB_CUDA_TRY(cudaEventElapsedTime(&ms, ev_fpass0, ev_fpass1));
+    stats.forward_ms += ms;
+    stats.step_ms += ms;
+    stats.step_launches += nt;
+    fpass_pending = false;
     return GB_OK;
+}
+
+int Solver::pipe_plan(const int *shots, int n) {
+    pipe_rounds = pipe_occ = 0;
+    if (!opt_pipe || sh == psv || !adj || nsfe <= 0 || !cluster_ok(shots, n, false)) return 0;
+    ClusterGeom g{};
+    if (!cluster_geometry(psv, n, &g)) return 0;
+    const int occ = cluster_occupancy(psv, g, nz);
+    if (occ < 1 || occ >= n) return 0;
+    const int rounds = (n + occ - 1) / occ;
+    while ((int)ev_fwd_round.size() < rounds) {
+        cudaEvent_t a = nullptr, b = nullptr;
+        GB_CUDA_TRY(cudaEventCreateWithFlags(&a, cudaEventDisableTiming));
+        GB_CUDA_TRY(cudaEventCreateWithFlags(&b, cudaEventDisableTiming));
+        ev_fwd_round.push_back(a);
+        ev_mis_round.push_back(b);
+    }
+    pipe_occ = occ;
+    pipe_rounds = rounds;
+    return rounds;
 }
 
 int Solver::forward(const int *shots, int n, bool ckpt_on, bool record_u, bool snapshot) {

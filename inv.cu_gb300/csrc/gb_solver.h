@@ -144,6 +144,23 @@ struct Solver {
     mutable std::map<long long, std::pair<bool, ClusterGeom>> cluster_cache;
     bool cluster_ok(const int *shots, int n, bool snapshot) const;
     int run_cluster_pass(int kind, int n);
+
+    // Pipelined gradient of one batch (cluster path, one wave system, more
+    // shots than resident clusters): with pipe_on, the forward pass launches
+    // one round of pipe_occ shots at a time, records ev_fwd_round[r] after
+    // each and returns without waiting; the caller runs round r's misfit on
+    // st_side after that event and records ev_mis_round[r]; the adjoint's
+    // round r waits for it. The next synchronising pass books the forward's
+    // time (ev_fpass0/1).
+    int opt_pipe = 1;
+    bool pipe_on = false;
+    int pipe_rounds = 0, pipe_occ = 0;
+    std::vector<cudaEvent_t> ev_fwd_round, ev_mis_round;
+    cudaEvent_t ev_fpass0 = nullptr, ev_fpass1 = nullptr;
+    bool fpass_pending = false;
+    // rounds of a pipelined gradient of these shots (0: not pipelined)
+    int pipe_plan(const int *shots, int n);
+    int book_forward_pass();
     int export_snapshot(int it, int isrc, int par);
     int export_data(const std::string &comp, const float *d_data, int n);
     void invalidate_graphs();

@@ -104,3 +104,32 @@ def test_c5_grid_bulk_loads_equal_cp_async(gpu, orc):
         np.testing.assert_array_equal(res[0][0][c], res[1][0][c])
     for n in ("k_lambda", "k_mu", "k_rho"):
         np.testing.assert_array_equal(res[0][1][n], res[1][1][n])
+
+
+@pytest.mark.parametrize("kind", [1, 0])
+def test_c2_pipelined_gradient_identical(gpu, orc, kind):
+    """The C2 shapes with 16 shots take two rounds of resident clusters: the
+    pipelined gradient (each round's misfit overlapping the next forward round
+    and the previous adjoint round) gives the same misfit value and kernels,
+    bit for bit, as forward, misfit and adjoint run one after another."""
+    h = 12.5
+    case = surface_receivers(cases.make_case(wave="sh", nx=681, nz=141, nt=400, nsrc=16, dx=h, dt=1e-3, f0=8.0,
+                                             abs_width=20, sfe=10, seed=2), h)
+    pert = dict(case)
+    pert["vs"] = (case["vs"] * 1.02).astype(np.float32)
+    cfg, sol = cases.gpu_solver(gpu, pert)
+    sol.run_forward_batch(list(range(16)))
+    obs = np.stack([sol.out("y", slot=b) for b in range(16)])
+    sol.close()
+    out = []
+    for pipe in (1, 0):
+        cfg, sol = cases.gpu_solver(gpu, case)
+        sol.set_option("pipeline", pipe)
+        sol.set_option("batch", 16)
+        m = gpu.Misfit.from_obs(kind, sol, {"y": obs})
+        val = m.run(kernel=True)
+        out.append((val, sol.kernels()))
+        sol.close()
+    assert out[0][0] == out[1][0]
+    for n in ("k_mu", "k_rho"):
+        np.testing.assert_array_equal(out[0][1][n], out[1][1][n])
