@@ -1129,8 +1129,12 @@ int Solver::pipe_plan(const int *shots, int n) {
     const int rounds = (n + occ - 1) / occ;
     while ((int)ev_fwd_round.size() < rounds) {
         cudaEvent_t a = nullptr, b = nullptr;
-        GB_CUDA_TRY(cudaEventCreateWithFlags(&a, cudaEventDisableTiming));
-        GB_CUDA_TRY(cudaEventCreateWithFlags(&b, cudaEventDisableTiming));
+        if (cudaEventCreateWithFlags(&a, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&b, cudaEventDisableTiming) != cudaSuccess) {
+            (void)cudaGetLastError();  // no pipelining without its events
+            if (a) cudaEventDestroy(a);
+            return 0;
+        }
         ev_fwd_round.push_back(a);
         ev_mis_round.push_back(b);
     }

@@ -158,7 +158,8 @@ struct Solver {
     std::vector<cudaEvent_t> ev_fwd_round, ev_mis_round;
     cudaEvent_t ev_fpass0 = nullptr, ev_fpass1 = nullptr;
     bool fpass_pending = false;
-    // rounds of a pipelined gradient of these shots (0: not pipelined)
+    // rounds of a pipelined gradient of these shots (0: not pipelined;
+    // never an error code)
     int pipe_plan(const int *shots, int n);
     int book_forward_pass();
     int export_snapshot(int it, int isrc, int par);
