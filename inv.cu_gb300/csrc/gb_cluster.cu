@@ -305,6 +305,10 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
     }
 
     unsigned rb = (unsigned)rbase, sq = (unsigned)srcq, qn = (unsigned)nq;
+    // per-thread flags: 1 / 2 pushes to the left / right neighbour, 4 / 8 z
+    // parts of the stress divergence / velocity gradient, 16 / 32 a thread
+    // group to the left / right, 64 record displacement, 128 push displacement
+    // ghosts (in-pass accumulation), 256 the warp holds receivers
     unsigned fl = (edge_l ? 1u : 0u) | (edge_r ? 2u : 0u) | (zS ? 4u : 0u) | (zV ? 8u : 0u) | (grp > 0 ? 16u : 0u) |
                   (grp < G - 1 ? 32u : 0u) | (S.record_u ? 64u : 0u) | ((ADJ && !snap) ? 128u : 0u) |
                   (__any_sync(__activemask(), rmask != 0u) ? 256u : 0u);
