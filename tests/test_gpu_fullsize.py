@@ -106,30 +106,36 @@ def test_c5_grid_bulk_loads_equal_cp_async(gpu, orc):
         np.testing.assert_array_equal(res[0][1][n], res[1][1][n])
 
 
-@pytest.mark.parametrize("kind", [1, 0])
-def test_c2_pipelined_gradient_identical(gpu, orc, kind):
-    """The C2 shapes with 16 shots take two rounds of resident clusters: the
-    pipelined gradient (each round's misfit overlapping the next forward round
-    and the previous adjoint round) gives the same misfit value and kernels,
-    bit for bit, as forward, misfit and adjoint run one after another."""
+@pytest.mark.parametrize("kind,wave", [(1, "sh"), (0, "sh"), (1, "psv")])
+def test_c2_pipelined_gradient_identical(gpu, orc, kind, wave):
+    """The C2 shapes with 16 shots take more than one round of resident
+    clusters, SH and P-SV alike: the pipelined gradient (each round's misfit
+    overlapping the next forward round and the previous adjoint round) gives
+    the same misfit value and kernels, bit for bit, as forward, misfit and
+    adjoint run one after another."""
     h = 12.5
-    case = surface_receivers(cases.make_case(wave="sh", nx=681, nz=141, nt=400, nsrc=16, dx=h, dt=1e-3, f0=8.0,
+    nt = 400 if wave == "sh" else 200
+    case = surface_receivers(cases.make_case(wave=wave, nx=681, nz=141, nt=nt, nsrc=16, dx=h, dt=1e-3, f0=8.0,
                                              abs_width=20, sfe=10, seed=2), h)
+    comps = "y" if wave == "sh" else "xz"
+    names = ("k_mu", "k_rho") if wave == "sh" else ("k_lambda", "k_mu", "k_rho")
     pert = dict(case)
     pert["vs"] = (case["vs"] * 1.02).astype(np.float32)
     cfg, sol = cases.gpu_solver(gpu, pert)
+    sol.set_option("batch", 16)
     sol.run_forward_batch(list(range(16)))
-    obs = np.stack([sol.out("y", slot=b) for b in range(16)])
+    obs = {c: np.stack([sol.out(c, slot=b) for b in range(16)]) for c in comps}
     sol.close()
     out = []
     for pipe in (1, 0):
         cfg, sol = cases.gpu_solver(gpu, case)
         sol.set_option("pipeline", pipe)
         sol.set_option("batch", 16)
-        m = gpu.Misfit.from_obs(kind, sol, {"y": obs})
+        m = gpu.Misfit.from_obs(kind, sol, obs)
         val = m.run(kernel=True)
+        assert sol.stats().tile_tz < 0, "the cluster path did not run"
         out.append((val, sol.kernels()))
         sol.close()
     assert out[0][0] == out[1][0]
-    for n in ("k_mu", "k_rho"):
+    for n in names:
         np.testing.assert_array_equal(out[0][1][n], out[1][1][n])
