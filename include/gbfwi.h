@@ -240,13 +240,21 @@ void gb_misfit_destroy(gb_misfit *m);
  * Replaces class Optimizer (optimizer/optimizer.h) with NLCG (optimizer = 0,
  * optimizer/nlcg.h) and L-BFGS (optimizer = 1, optimizer/lbfgs.h). Dot
  * products, norms and line-search quantities are FP64 on the GPU; the L-BFGS
- * history stays in device memory. */
+ * history stays in device memory, rotated as the reference rotates it
+ * (optimizer/lbfgs.h:29-36: once full, its oldest slot shares the newest
+ * pair's buffer). */
 typedef struct gb_optimizer gb_optimizer;
 gb_optimizer *gb_optimizer_create(const gb_config *cfg, gb_solver *s, gb_misfit *m);
 /* Optimizer::run (optimizer/optimizer.h:428-467), same stdout lines. */
 int gb_optimizer_run(gb_optimizer *o);
 /* Misfit history of the last run: value of each accepted iteration. */
 int gb_optimizer_history(gb_optimizer *o, double *out, int n);
+/* Every misfit evaluation of the last run, in order, as (kind, alpha,
+ * value) triples into out[3*n]: kind 1 = the gradient evaluation that starts
+ * an iteration (misfit->run(true), optimizer/optimizer.h:433), 0 = a
+ * line-search step alpha (optimizer.h:383-389), 2 = the final misfit
+ * (optimizer.h:454). Returns the number of evaluations. */
+int gb_optimizer_evaluations(gb_optimizer *o, double *out, int n);
 void gb_optimizer_destroy(gb_optimizer *o);
 
 /* ----------------------------------------------------------------- Serving

@@ -120,6 +120,7 @@ def _declare(lib):
         "gb_optimizer_create": (_vp, [_vp, _vp, _vp]),
         "gb_optimizer_run": (ctypes.c_int, [_vp]),
         "gb_optimizer_history": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double), ctypes.c_int]),
+        "gb_optimizer_evaluations": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double), ctypes.c_int]),
         "gb_optimizer_destroy": (None, [_vp]),
         "gb_dot64": (ctypes.c_int, [_vp, _vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_double)]),
         "gb_amax64": (ctypes.c_int, [_vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_double)]),
@@ -522,6 +523,14 @@ class Optimizer:
         out = np.zeros(max(n, 1), np.float64)
         lib().gb_optimizer_history(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), n)
         return out[:n]
+
+    def evaluations(self) -> np.ndarray:
+        """[n, 3]: (kind, alpha, value) of every misfit evaluation of the
+        last run (kind 1 gradient, 0 line-search step, 2 final)."""
+        n = lib().gb_optimizer_evaluations(self._h, None, 0)
+        out = np.zeros(max(3 * n, 3), np.float64)
+        lib().gb_optimizer_evaluations(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), n)
+        return out[:3 * n].reshape(n, 3)
 
     def close(self):
         if getattr(self, "_h", None) and _lib is not None:

@@ -6,7 +6,9 @@
 // reductions on the GPU, line-search quantities are kept in double, the
 // quadratic fit is a small Householder least-squares solve in double on the
 // host (the reference ships a 4x3 system to cuSOLVER), and the L-BFGS history
-// stays in device memory instead of host RAM (optimizer/lbfgs.h:94-106).
+// stays in device memory instead of host RAM (optimizer/lbfgs.h:94-106). The
+// L-BFGS history rotation keeps the reference's slot aliasing (see
+// direction_lbfgs).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -35,10 +37,12 @@ struct gb_optimizer {
     std::vector<double> ls_lens, ls_vals, ls_gtg, ls_gtp;
     float *m_new[3] = {}, *g_new[3] = {};
     float *m_old[3] = {}, *g_old[3] = {}, *p_new[3] = {}, *p_old[3] = {};
-    std::vector<std::vector<float *>> S, Y;  // [mem][3] device vectors
+    std::vector<std::vector<float *>> S, Y;  // [mem][3] device vectors (slots may share buffers)
+    std::vector<float *> owned;             // every S/Y buffer, for release
     double *d_red = nullptr;
     double ref = 1.0;
     std::vector<double> history;
+    std::vector<double> evals;  // (kind, alpha, value) per misfit evaluation
     int err = GB_OK;
 
     size_t n() const { return s->ncell(); }
@@ -88,10 +92,13 @@ struct gb_optimizer {
         return std::acos(xy / std::sqrt(xx * yy));
     }
 
-    double evaluate(bool kernel) {
+    // kind: 1 gradient (start of an iteration), 0 line-search step, 2 final;
+    // alpha: the step the line search took to this model (0 otherwise)
+    double evaluate(bool kernel, int kind, double alpha) {
         double v = 0.0;
         int rc = gb_misfit_run(misfit, kernel, 0, &v);
         if (rc) err = rc;
+        evals.insert(evals.end(), {(double)kind, alpha, v});
         return v;
     }
 
@@ -182,8 +189,12 @@ struct gb_optimizer {
         polyfit(x + idx, f + idx, p, fitlen);
         if (p[0] <= 0) {
             std::cout << "  line search error" << std::endl;
-            // the reference leaves the step undefined here; keep the best point
+            // The reference leaves bracket's step uninitialised here (its fit
+            // is converted to float, optimizer.h:174-177, and p[0] underflows
+            // to 0 once steps reach ~1e20). The search ends at the best point
+            // evaluated, so that it cannot re-evaluate that point forever.
             x0 = x[argmin(f, n)];
+            return true;
         } else {
             x0 = -p[1] / (2 * p[0]);
             for (int i = 1; i < n; i++)
@@ -272,6 +283,7 @@ struct gb_optimizer {
     double calc_step(int step_count, double step_max, int &status) {
         return type == 0 ? bracket(step_count, step_max, status) : backtrack(step_count, step_max, status);
     }
+    long ls_cap() const { return std::max(1L, (long)inv_iteration * ls_step); }
     void push_ls(double len, double val) {
         if ((size_t)ls_count >= ls_lens.size()) {
             ls_lens.resize(ls_count + 1);
@@ -309,16 +321,22 @@ struct gb_optimizer {
         else
             alpha = calc_step(step_count, step_max, status);
         while (true) {
-            calc(m_new, 1, m_new, alpha - alpha_current, p_new);
-            alpha_current = alpha;
-            const double v = evaluate(false);
-            if (err) return -1;
-            push_ls(alpha, v);
-            eval_count++;
-            step_count++;
-            alpha = calc_step(step_count, step_max, status);
-            std::cout << "  step " << (step_count < 10 ? "0" : "") << step_count
-                      << "  misfit = " << (float)(ls_vals[ls_count - 1] / ref) << std::endl;
+            // The reference keeps inv_iteration * ls_step steps
+            // (optimizer.h:485-487) and writes past them after that; here a
+            // search that has used them all fails as one past ls_step does.
+            if (ls_count >= ls_cap()) status = -1;
+            if (status >= 0) {
+                calc(m_new, 1, m_new, alpha - alpha_current, p_new);
+                alpha_current = alpha;
+                const double v = evaluate(false, 0, alpha);
+                if (err) return -1;
+                push_ls(alpha, v);
+                eval_count++;
+                step_count++;
+                alpha = calc_step(step_count, step_max, status);
+                std::cout << "  step " << (step_count < 10 ? "0" : "") << step_count
+                          << "  misfit = " << (float)(ls_vals[ls_count - 1] / ref) << std::endl;
+            }
             if (status > 0) {
                 std::cout << "  alpha = " << (float)alpha << std::endl;
                 calc(m_new, 1, m_new, alpha - alpha_current, p_new);
@@ -377,8 +395,18 @@ struct gb_optimizer {
             std::cout << "  restarting LBFGS... [periodic restart]" << std::endl;
             return -1;
         }
-        std::rotate(S.begin(), S.end() - 1, S.end());
-        std::rotate(Y.begin(), Y.end() - 1, Y.end());
+        // lbfgs.h:29-36 binds a reference to the last slot, shifts the slots
+        // up by one (overwriting the last with its predecessor) and then puts
+        // what the reference now names into slot 0: after the rotation slot 0
+        // and slot mem-1 share one buffer, so once the memory is full the
+        // newest pair also stands in the oldest pair's place. Kept as is.
+        const int mem = (int)S.size();
+        for (int i = mem - 1; i > 0; i--) {
+            S[i] = S[i - 1];
+            Y[i] = Y[i - 1];
+        }
+        S[0] = S[mem - 1];
+        Y[0] = Y[mem - 1];
         calc(S[0].data(), 1, m_new, -1, m_old);
         calc(Y[0].data(), 1, g_new, -1, g_old);
         if (lbfgs_used < lbfgs_mem) lbfgs_used++;
@@ -418,10 +446,11 @@ struct gb_optimizer {
         if (!rc) rc = gb_export_model(reinterpret_cast<gb_solver *>(s), 0);
         if (rc) return rc;
         history.clear();
+        evals.clear();
         const clock_t t0 = clock();
         for (int iter = 0; iter < inv_iteration; iter++) {
             std::cout << "\nStarting iteration " << iter + 1 << " / " << inv_iteration << std::endl;
-            const double f = evaluate(true);
+            const double f = evaluate(true, 1, 0.0);
             if (err) return err;
             if (iter == 0) ref = f;
             eval_count += 2;
@@ -441,7 +470,7 @@ struct gb_optimizer {
             if (rc) return rc;
         }
         const float elapsed = (float)(clock() - t0) / CLOCKS_PER_SEC;
-        const double final_f = evaluate(false);
+        const double final_f = evaluate(false, 2, 0.0);
         if (err) return err;
         history.push_back(final_f);
         std::cout << "\nFinal misfit: " << (float)(final_f / ref) << std::endl;
@@ -512,8 +541,12 @@ gb_optimizer *gb_optimizer_create(const gb_config *cfg, gb_solver *sol, gb_misfi
         o->Y.assign(std::max(o->lbfgs_mem, 1), std::vector<float *>(3, nullptr));
         for (int q = 0; q < o->lbfgs_mem && ok; q++)
             for (int ip = 0; ip < 3 && ok; ip++)
-                if (o->inv[ip])
-                    ok = cudaMalloc(&o->S[q][ip], bytes) == cudaSuccess && cudaMalloc(&o->Y[q][ip], bytes) == cudaSuccess;
+                if (o->inv[ip]) {
+                    ok = cudaMalloc(&o->S[q][ip], bytes) == cudaSuccess;
+                    if (ok) o->owned.push_back(o->S[q][ip]);
+                    ok = ok && cudaMalloc(&o->Y[q][ip], bytes) == cudaSuccess;
+                    if (ok) o->owned.push_back(o->Y[q][ip]);
+                }
     }
     if (!ok) {
         set_error("gb_optimizer_create: device allocation failed");
@@ -537,15 +570,20 @@ int gb_optimizer_history(gb_optimizer *o, double *out, int n) {
     return (int)o->history.size();
 }
 
+int gb_optimizer_evaluations(gb_optimizer *o, double *out, int n) {
+    if (!o) return 0;
+    const int cnt = (int)(o->evals.size() / 3);
+    const int k = std::min(n, cnt);
+    for (int i = 0; i < 3 * k && out; i++) out[i] = o->evals[i];
+    return cnt;
+}
+
 void gb_optimizer_destroy(gb_optimizer *o) {
     if (!o) return;
     if (o->s && o->s->st) cudaStreamSynchronize(o->s->st);
     for (int ip = 0; ip < 3; ip++)
         for (float *v : {o->m_old[ip], o->g_old[ip], o->p_new[ip], o->p_old[ip]}) cudaFree(v);
-    for (auto &v : o->S)
-        for (float *p : v) cudaFree(p);
-    for (auto &v : o->Y)
-        for (float *p : v) cudaFree(p);
+    for (float *p : o->owned) cudaFree(p);
     cudaFree(o->d_red);
     delete o;
 }

@@ -601,3 +601,44 @@ def ref_misfit(kind: int, syn, obs, dt: float):
     _ref_check(ref_lib().ref_misfit(int(kind), int(ntr), int(nt), ctypes.c_double(dt), _p(syn), _p(obs), _p(ad),
                                     _p(val)), "ref_misfit")
     return val, ad
+
+
+def ref_calc(c, ka, a, kb=None, b=None, nx=None, nz=None):
+    """device::calc (lib/device.h:157-176) with the reference's kernel, in
+    place into c (a float32 grid of nx*nz cells): c = ka*a + kb*b, or ka*a."""
+    ca = _cast(a, np.float32)
+    cb = None if b is None else _cast(b, np.float32)
+    out = np.empty(ca.size, np.float32)
+    _ref_check(ref_lib().ref_calc(_p(out), ctypes.c_float(ka), _p(ca), ctypes.c_float(0 if kb is None else kb),
+                                  _p(cb), int(nx), int(nz)), "ref_calc")
+    c[...] = out.reshape(c.shape)
+
+
+def ref_dot(a, b) -> np.float32:
+    """device::dot (lib/device.h:188-192): cublasSdot."""
+    a = _cast(a, np.float32)
+    b = _cast(b, np.float32)
+    out = ctypes.c_float()
+    _ref_check(ref_lib().ref_dot(_p(a), _p(b), int(a.size), ctypes.byref(out)), "ref_dot")
+    return np.float32(out.value)
+
+
+def ref_amax(a) -> np.float32:
+    """device::amax (lib/device.h:178-182): cublasIsamax, then |a[i]|."""
+    a = _cast(a, np.float32)
+    out = ctypes.c_float()
+    _ref_check(ref_lib().ref_amax(_p(a), int(a.size), ctypes.byref(out)), "ref_amax")
+    return np.float32(out.value)
+
+
+def ref_polyfit(x, y):
+    """Optimizer::polyfit + solveQR (optimizer/optimizer.h:108-172) with
+    cuSOLVER, the reference's reduceSystem kernel and cuBLAS: the least-squares
+    quadratic through (x, y) as float64 (p0, p1, p2), and the status of the
+    reference's cusolverDnDormqr call (0: success)."""
+    x = _cast(x, np.float64)
+    y = _cast(y, np.float64)
+    p = np.zeros(3, np.float64)
+    st = ctypes.c_int(-1)
+    _ref_check(ref_lib().ref_polyfit(_p(x), _p(y), int(x.size), _p(p), ctypes.byref(st)), "ref_polyfit")
+    return p, st.value

@@ -16,6 +16,11 @@
 //   GaussianFilter         filter/gaussian.h:37-61
 //   WaveformMisfit::run    misfit/waveform.h:35-40 (taper: waveform.h:44-51)
 //   EnvelopeMisfit::run    misfit/envelope.h:58-90 (hilbert: envelope.h:91-98)
+//   Optimizer primitives   optimizer/optimizer.h:49-107 (p_calc, p_dot, p_amax
+//                          over one parameter: device::calc/dot/amax,
+//                          lib/device.h:157-192) and polyfit/solveQR
+//                          (optimizer.h:108-178, cuSOLVER QR, reduceSystem,
+//                          cuBLAS triangular solve)
 // (the misfits with cuFFT and cuBLAS as the reference calls them, one trace
 // at a time, device::amax/norm from lib/device.h:170-180)
 // with the reference's launch shapes (Dim::init, lib/device.h:46-57, with
@@ -26,7 +31,9 @@
 #include <cublas_v2.h>
 #include <cuda_runtime.h>
 #include <cufft.h>
+#include <cusolverDn.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -53,7 +60,7 @@ Dim make_dim(int nx, int nz) { return Dim{nx, nz, nx, nz, nx * nz}; }
 enum K {
     K_DIVSY, K_DIVSXZ, K_DIVVY, K_DIVVXZ, K_UPDSY, K_UPDSXZ, K_UPDVY, K_UPDVXZ, K_ADDSTF, K_SAVEREC,
     K_IRHOY, K_IRHOXZ, K_IMUY, K_IMUXZ, K_ILAMXZ, K_ABS, K_GINIT, K_GX, K_GZ,
-    K_TAPER, K_DIFF, K_HILB, K_R2C, K_C2IMAG, K_C2ABS, K_ETMP, K_ESTF, K_MUL, K_AXPBY, K_N
+    K_TAPER, K_DIFF, K_HILB, K_R2C, K_C2IMAG, K_C2ABS, K_ETMP, K_ESTF, K_MUL, K_AXPBY, K_SCALE, K_REDSYS, K_N
 };
 // names as nvcc reports them for the reference's kernels
 const char *kNames[K_N] = {
@@ -86,11 +93,14 @@ const char *kNames[K_N] = {
     "_ZN15_EnvelopeMisfit18prepareEnvelopeSTFEPfS0_S0_S0_m",
     "_ZN6device5_calcEPfS0_S0_3Dim",
     "_ZN6device5_calcEPffS0_fS0_3Dim",
+    "_ZN6device5_calcEPffS0_3Dim",
+    "_ZN10_Optimizer12reduceSystemEPKdPdS1_S2_ii",
 };
 
 cudaLibrary_t g_lib = nullptr;
 cudaKernel_t g_k[K_N] = {};
 std::string g_err;
+cublasHandle_t g_cb = nullptr;  // device::cublas_handle of the optimizer primitives
 
 int fail(const std::string &what, cudaError_t e) {
     g_err = what + ": " + cudaGetErrorString(e);
@@ -484,6 +494,125 @@ int ref_misfit(int type, int ntr, int nt, double dt_in, const float *syn, const 
     }
     REF_TRY(cudaDeviceSynchronize());
     return to_host(adstf, dad, n);
+}
+
+// device::calc (lib/device.h:157-176) on host arrays of one nx*nz grid,
+// launched as solver->dim (nx blocks of nz threads): c = ka*a + kb*b, or
+// c = ka*a when b is null. c may be a or b (the kernels are elementwise).
+int ref_calc(float *c, float ka, const float *a, float kb, const float *b, int nx, int nz) {
+    if (!g_lib || nx < 1 || nz < 1 || nz > 1024) return 1;
+    const size_t n = (size_t)nx * nz;
+    Bufs bf;
+    float *dc = bf.alloc<float>(n), *da = bf.alloc<float>(n), *db = bf.alloc<float>(n);
+    if (!dc || !da || !db || to_dev(da, a, n) || (b && to_dev(db, b, n))) return 1;
+    Dim dim = make_dim(nx, nz);
+    if (b) {
+        void *args[] = {&dc, &ka, &da, &kb, &db, &dim};
+        if (launch(K_AXPBY, dim.dg, dim.db, args)) return 1;
+    } else {
+        void *args[] = {&dc, &ka, &da, &dim};
+        if (launch(K_SCALE, dim.dg, dim.db, args)) return 1;
+    }
+    REF_TRY(cudaDeviceSynchronize());
+    return to_host(c, dc, n);
+}
+
+// device::dot (lib/device.h:188-192): cublasSdot, FP32 result.
+int ref_dot(const float *a, const float *b, int n, float *out) {
+    if (!g_lib || n < 1) return 1;
+    if (!g_cb && cublasCreate(&g_cb) != CUBLAS_STATUS_SUCCESS) {
+        g_err = "cublasCreate";
+        return 1;
+    }
+    Bufs bf;
+    float *da = bf.alloc<float>(n), *db = bf.alloc<float>(n);
+    if (!da || !db || to_dev(da, a, n) || to_dev(db, b, n)) return 1;
+    if (cublasSdot(g_cb, n, da, 1, db, 1, out) != CUBLAS_STATUS_SUCCESS) {
+        g_err = "cublasSdot";
+        return 1;
+    }
+    return 0;
+}
+
+// device::amax (lib/device.h:178-182): cublasIsamax, then |a[index - 1]|.
+int ref_amax(const float *a, int n, float *out) {
+    if (!g_lib || n < 1) return 1;
+    if (!g_cb && cublasCreate(&g_cb) != CUBLAS_STATUS_SUCCESS) {
+        g_err = "cublasCreate";
+        return 1;
+    }
+    Bufs bf;
+    float *da = bf.alloc<float>(n);
+    int index = 0;
+    float v = 0.f;
+    if (!da || to_dev(da, a, n)) return 1;
+    if (cublasIsamax(g_cb, n, da, 1, &index) != CUBLAS_STATUS_SUCCESS || index < 1 || index > n) {
+        g_err = "cublasIsamax";
+        return 1;
+    }
+    REF_TRY(cudaMemcpy(&v, da + index - 1, 4, cudaMemcpyDeviceToHost));
+    *out = std::fabs(v);
+    return 0;
+}
+
+// Optimizer::polyfit(double*) + solveQR (optimizer/optimizer.h:108-172): the
+// least-squares quadratic p[0] x^2 + p[1] x + p[2] through n points, by
+// cuSOLVER's QR of the n x 3 system, Q^T y, the reference's reduceSystem
+// kernel and cublasDtrsm, with the geqrf workspace size for both cuSOLVER
+// calls as the reference passes it. The reference also multiplies Q into an
+// unused, uninitialised matrix (optimizer.h:126-127); that product is not
+// formed here. *ormqr_status: what cusolverDnDormqr returned (the reference
+// does not look).
+int ref_polyfit(const double *x, const double *y, int n, double *p, int *ormqr_status) {
+    // n >= 3: reduceSystem reads the top 3 x 3 block of the n-row factor
+    if (!g_lib || n < 3 || n > 1024) {
+        g_err = "ref_polyfit: 3 to 1024 points";
+        return 1;
+    }
+    if (!g_cb && cublasCreate(&g_cb) != CUBLAS_STATUS_SUCCESS) {
+        g_err = "cublasCreate";
+        return 1;
+    }
+    const int nrows = n, ncols = 3, k = std::min(nrows, ncols);
+    std::vector<double> A(3 * (size_t)n);
+    for (int i = 0; i < n; i++) {
+        A[i] = x[i] * x[i];
+        A[i + n] = x[i];
+        A[i + 2 * n] = 1;
+    }
+    cusolverDnHandle_t sh = nullptr;
+    if (cusolverDnCreate(&sh) != CUSOLVER_STATUS_SUCCESS) {
+        g_err = "cusolverDnCreate";
+        return 1;
+    }
+    int rc = 1;
+    Bufs bf;
+    int *info = bf.alloc<int>(1);
+    double *dA = bf.alloc<double>((size_t)nrows * ncols), *dTAU = bf.alloc<double>(k);
+    double *dC = bf.alloc<double>((size_t)nrows * nrows);  // zeroed, as device::init(d_C, 0.0, dim)
+    double *dR = bf.alloc<double>(ncols * ncols), *dB = bf.alloc<double>(ncols * ncols);
+    int work_size = 0;
+    double *work = nullptr;
+    if (info && dA && dTAU && dC && dR && dB &&
+        cudaMemcpy(dA, A.data(), A.size() * 8, cudaMemcpyHostToDevice) == cudaSuccess &&
+        cusolverDnDgeqrf_bufferSize(sh, nrows, ncols, dA, nrows, &work_size) == CUSOLVER_STATUS_SUCCESS &&
+        (work = bf.alloc<double>(work_size > 0 ? work_size : 1)) != nullptr &&
+        cusolverDnDgeqrf(sh, nrows, ncols, dA, nrows, dTAU, work, work_size, info) == CUSOLVER_STATUS_SUCCESS &&
+        cudaMemcpy(dC, y, (size_t)nrows * 8, cudaMemcpyHostToDevice) == cudaSuccess) {
+        *ormqr_status = (int)cusolverDnDormqr(sh, CUBLAS_SIDE_LEFT, CUBLAS_OP_T, nrows, ncols, k, dA, nrows, dTAU,
+                                              dC, nrows, work, work_size, info);
+        int M = nrows, N = ncols;
+        void *args[] = {&dA, &dR, &dC, &dB, &M, &N};
+        const double one = 1.;
+        if (!launch(K_REDSYS, ncols, ncols, args) &&
+            cublasDtrsm(g_cb, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, ncols,
+                        ncols, &one, dR, ncols, dB, ncols) == CUBLAS_STATUS_SUCCESS &&
+            cudaMemcpy(p, dB, ncols * 8, cudaMemcpyDeviceToHost) == cudaSuccess)
+            rc = 0;
+    }
+    cusolverDnDestroy(sh);
+    if (rc && g_err.empty()) g_err = "ref_polyfit";
+    return rc;
 }
 
 }  // extern "C"
