@@ -239,7 +239,8 @@ void gb_misfit_destroy(gb_misfit *m);
 /* --------------------------------------------------------------- Optimizer
  * Replaces class Optimizer (optimizer/optimizer.h) with NLCG (optimizer = 0,
  * optimizer/nlcg.h) and L-BFGS (optimizer = 1, optimizer/lbfgs.h). Dot
- * products, norms and line-search quantities are FP64 on the GPU; the L-BFGS
+ * products and norms are FP64 on the GPU; the line search keeps its steps
+ * and history in float, as the reference does; the L-BFGS
  * history stays in device memory, rotated as the reference rotates it
  * (optimizer/lbfgs.h:29-36: once full, its oldest slot shares the newest
  * pair's buffer). */
@@ -255,6 +256,17 @@ int gb_optimizer_history(gb_optimizer *o, double *out, int n);
  * line-search step alpha (optimizer.h:383-389), 2 = the final misfit
  * (optimizer.h:454). Returns the number of evaluations. */
 int gb_optimizer_evaluations(gb_optimizer *o, double *out, int n);
+/* The line-search step rule alone, on the host (no device work): the next
+ * step and status (1 accept, 0 continue, -1 failed; -2 invalid input) that
+ * Optimizer::bracket (optimizer = 0, NLCG) or backtrack (1, L-BFGS),
+ * optimizer/optimizer.h:267-357, give for a search history: lens/vals the
+ * ls_count entries of ls_lens/ls_vals, gtg/gtp the inv_count entries of
+ * ls_gtg/ls_gtp, step_count steps taken in the current search. The rule of
+ * gb_optimizer_run: history, slopes and steps in float, as the reference
+ * keeps them (the inputs are rounded to float). */
+double gb_linesearch_step(int optimizer, const double *lens, const double *vals, int ls_count, const double *gtg,
+                          const double *gtp, int inv_count, int step_count, int ls_step, double ls_thresh,
+                          double step_max, int *status);
 void gb_optimizer_destroy(gb_optimizer *o);
 
 /* ----------------------------------------------------------------- Serving

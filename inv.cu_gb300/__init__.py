@@ -121,6 +121,9 @@ def _declare(lib):
         "gb_optimizer_run": (ctypes.c_int, [_vp]),
         "gb_optimizer_history": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double), ctypes.c_int]),
         "gb_optimizer_evaluations": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double), ctypes.c_int]),
+        "gb_linesearch_step": (ctypes.c_double, [ctypes.c_int, _vp, _vp, ctypes.c_int, _vp, _vp, ctypes.c_int,
+                                                 ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                                 ctypes.POINTER(ctypes.c_int)]),
         "gb_optimizer_destroy": (None, [_vp]),
         "gb_dot64": (ctypes.c_int, [_vp, _vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_double)]),
         "gb_amax64": (ctypes.c_int, [_vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_double)]),
@@ -504,6 +507,22 @@ class Misfit:
 
     def __del__(self):
         self.close()
+
+
+def linesearch_step(optimizer: int, lens, vals, gtg, gtp, step_count: int, ls_step: int, ls_thresh: float,
+                    step_max: float):
+    """The line-search step rule of the optimizer (bracket for NLCG,
+    backtrack for L-BFGS, optimizer/optimizer.h:267-357) on a history, on the
+    host: returns (step, status)."""
+    d = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+    lens, vals, gtg, gtp = d(lens), d(vals), d(gtg), d(gtp)
+    st = ctypes.c_int(-2)
+    a = lib().gb_linesearch_step(int(optimizer), lens.ctypes.data_as(_vp), vals.ctypes.data_as(_vp), int(lens.size),
+                                 gtg.ctypes.data_as(_vp), gtp.ctypes.data_as(_vp), int(gtg.size), int(step_count),
+                                 int(ls_step), float(ls_thresh), float(step_max), ctypes.byref(st))
+    if st.value == -2:
+        raise GbError("linesearch_step: " + last_error())
+    return a, st.value
 
 
 class Optimizer:

@@ -36,7 +36,7 @@ def _nvcc() -> str:
 
 
 def _flags(ptxas: bool):
-    f = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-Wall,-Wno-unused-function",
+    f = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-Wall,-Wno-unused-function,-ffp-contract=off",
                 "-I", os.path.join(ROOT, "include"), "-I", CSRC]
     if ptxas:
         f += ["-Xptxas", "-v"]

@@ -3,12 +3,14 @@
 //
 // The decision rules, restart conditions and printed lines are the
 // reference's. What changes: model-vector dot products and max|.| are FP64
-// reductions on the GPU, line-search quantities are kept in double, the
-// quadratic fit is a small Householder least-squares solve in double on the
-// host (the reference ships a 4x3 system to cuSOLVER), and the L-BFGS history
-// stays in device memory instead of host RAM (optimizer/lbfgs.h:94-106). The
-// L-BFGS history rotation keeps the reference's slot aliasing (see
-// direction_lbfgs).
+// reductions on the GPU (rounded to float where the line search stores them,
+// as the reference's cuBLAS results are float), the quadratic fit is a small
+// Householder least-squares solve in double on the host (the reference ships
+// a 4x3 system to cuSOLVER), and the L-BFGS history stays in device memory
+// instead of host RAM (optimizer/lbfgs.h:94-106). The line search keeps and
+// computes its steps, history and slopes in float, as the reference does
+// (see bracket). The L-BFGS history rotation keeps the reference's slot
+// aliasing (see direction_lbfgs).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -28,13 +30,13 @@ struct gb_optimizer {
     int type = 0;  // 0 NLCG, 1 L-BFGS
     bool inv[3] = {false, false, false};
     int inv_cycle = 0, inv_iteration = 0, ls_step = 0;
-    double ls_step_max = 0, ls_step_init = 0, ls_thresh = 0;
+    float ls_step_max = 0, ls_step_init = 0, ls_thresh = 0;
     int nlcg_type = 0;
     double nlcg_thresh = 0;
     int lbfgs_mem = 0, lbfgs_used = 0;
     double lbfgs_thresh = 0;
     long eval_count = 0, inv_count = 0, ls_count = 0;
-    std::vector<double> ls_lens, ls_vals, ls_gtg, ls_gtp;
+    std::vector<float> ls_lens, ls_vals, ls_gtg, ls_gtp;
     float *m_new[3] = {}, *g_new[3] = {};
     float *m_old[3] = {}, *g_old[3] = {}, *p_new[3] = {}, *p_old[3] = {};
     std::vector<std::vector<float *>> S, Y;  // [mem][3] device vectors (slots may share buffers)
@@ -102,8 +104,14 @@ struct gb_optimizer {
         return v;
     }
 
-    // ---- line search helpers (optimizer/optimizer.h:151-357)
-    // Least-squares quadratic p0 x^2 + p1 x + p2 through n points.
+    // ---- line search (optimizer/optimizer.h:151-357), in float like the
+    // reference's: a rule that took its decisions in double would part from
+    // the reference's on the same history, and not only by chance: after the
+    // first step is clamped to 0.618034 * step_max, the golden-ratio
+    // extrapolation 1.618034 * x lands within one float ulp of step_max, and
+    // whether it exceeds step_max decides between evaluating there (status 0)
+    // and accepting it unevaluated (status 1).
+    // Least-squares quadratic p0 x^2 + p1 x + p2 through n points (double).
     static void polyfit(const double *x, const double *y, double *p, int n) {
         double A[4][3], b[4];
         for (int i = 0; i < n; i++) {
@@ -142,7 +150,7 @@ struct gb_optimizer {
         for (int k = std::min(nc, n); k < nc; k++) p[k] = 0;
     }
 
-    int history_of(int step_count, std::vector<double> &x, std::vector<double> &f) {
+    int history_of(int step_count, std::vector<float> &x, std::vector<float> &f) {
         x.resize(step_count + 1);
         f.resize(step_count + 1);
         for (int i = 0; i < step_count + 1; i++) {
@@ -162,8 +170,8 @@ struct gb_optimizer {
         if (update_count > 0) update_count--;
         return update_count;
     }
-    static int argmin(const double *f, int n) {
-        double m = f[0];
+    static int argmin(const float *f, int n) {
+        float m = f[0];
         int idx = 0;
         for (int i = 1; i < n; i++)
             if (f[i] < m) {
@@ -172,47 +180,57 @@ struct gb_optimizer {
             }
         return idx;
     }
-    static bool check_bracket(const double *f, int n) {
+    static bool check_bracket(const float *f, int n) {
         const int imin = argmin(f, n);
-        const double fmin = f[imin];
+        const float fmin = f[imin];
         if (fmin < f[0])
             for (int i = imin; i < n; i++)
                 if (f[i] > fmin) return true;
         return false;
     }
-    bool good_enough(const double *x, const double *f, int n, double &x0) {
-        const double thresh = std::log10(ls_thresh);
+    bool good_enough(const float *x, const float *f, int n, float &x0) {
+        const float thresh = std::log10(ls_thresh);
         if (!check_bracket(f, n)) return false;
-        double p[3];
         const int idx = argmin(f, n) - 1;
         const int fitlen = std::min(4, n - idx);
-        polyfit(x + idx, f + idx, p, fitlen);
-        if (p[0] <= 0) {
+        double xd[4], fd[4], p[3];
+        for (int i = 0; i < fitlen; i++) {
+            xd[i] = x[idx + i];
+            fd[i] = f[idx + i];
+        }
+        polyfit(xd, fd, p, fitlen);
+        const float p0 = (float)p[0], p1 = (float)p[1];  // optimizer.h:174-177
+        if (p0 > 0) {
+            x0 = -p1 / (2 * p0);
+        } else if (p[0] > 0) {
+            // The float coefficient underflowed (steps of ~1e20: a model of
+            // ~1e10 over gradients of ~1e-10): the reference then prints "line
+            // search error" and leaves bracket's step uninitialised. The
+            // double fit's minimum is taken instead.
+            x0 = (float)(-p[1] / (2 * p[0]));
+        } else {
+            // No positive curvature: the reference's step is uninitialised
+            // here too. The search ends at the best point evaluated, so that
+            // it cannot re-evaluate that point forever.
             std::cout << "  line search error" << std::endl;
-            // The reference leaves bracket's step uninitialised here (its fit
-            // is converted to float, optimizer.h:174-177, and p[0] underflows
-            // to 0 once steps reach ~1e20). The search ends at the best point
-            // evaluated, so that it cannot re-evaluate that point forever.
             x0 = x[argmin(f, n)];
             return true;
-        } else {
-            x0 = -p[1] / (2 * p[0]);
-            for (int i = 1; i < n; i++)
-                if (std::fabs(std::log10(x[i] / x0)) < thresh) return true;
         }
+        for (int i = 1; i < n; i++)
+            if (std::fabs(std::log10(x[i] / x0)) < thresh) return true;
         return false;
     }
-    static double backtrack2(double f0, double g0, double x1, double f1, double b1, double b2) {
-        double x2 = -g0 * x1 * x1 / (2 * (f1 - f0 - g0 * x1));
+    static float backtrack2(float f0, float g0, float x1, float f1, float b1, float b2) {
+        float x2 = -g0 * x1 * x1 / (2 * (f1 - f0 - g0 * x1));
         if (x2 > b2 * x1)
             x2 = b2 * x1;
         else if (x2 < b1 * x1)
             x2 = b1 * x1;
         return x2;
     }
-    double bracket(int step_count, double step_max, int &status) {
-        std::vector<double> x, f;
-        double alpha = 0;
+    float bracket(int step_count, float step_max, int &status) {
+        std::vector<float> x, f;
+        float alpha = 0;
         const int update_count = history_of(step_count, x, f);
         if (step_count == 0) {
             if (update_count == 0) {
@@ -238,8 +256,8 @@ struct gb_optimizer {
                 alpha = 1.618034 * x[step_count];
                 status = 0;
             } else {
-                const double slope = ls_gtp[inv_count - 1] / ls_gtg[inv_count - 1];
-                alpha = backtrack2(f[0], slope, x[1], f[1], 0.1, 0.5);
+                const float slope = ls_gtp[inv_count - 1] / ls_gtg[inv_count - 1];
+                alpha = backtrack2(f[0], slope, x[1], f[1], 0.1f, 0.5f);
                 status = 0;
             }
         } else {
@@ -257,22 +275,22 @@ struct gb_optimizer {
         }
         return alpha;
     }
-    double backtrack(int step_count, double step_max, int &status) {
-        std::vector<double> x, f;
+    float backtrack(int step_count, float step_max, int &status) {
+        std::vector<float> x, f;
         const int update_count = history_of(step_count, x, f);
         const int idx = argmin(f.data(), step_count + 1);
-        double alpha;
+        float alpha;
         if (update_count == 0) {
             alpha = bracket(step_count, step_max, status);
         } else if (step_count == 0) {
-            alpha = std::min(1.0, step_max);
+            alpha = std::min(1.0f, step_max);
             status = 0;
         } else if (f[idx] < f[0]) {
             alpha = x[idx];
             status = 1;
         } else if (step_count <= ls_step) {
-            const double slope = ls_gtp[inv_count - 1] / ls_gtg[inv_count - 1];
-            alpha = backtrack2(f[0], slope, x[1], f[1], 0.1, 0.5);
+            const float slope = ls_gtp[inv_count - 1] / ls_gtg[inv_count - 1];
+            alpha = backtrack2(f[0], slope, x[1], f[1], 0.1f, 0.5f);
             status = 0;
         } else {
             alpha = 0;
@@ -280,11 +298,11 @@ struct gb_optimizer {
         }
         return alpha;
     }
-    double calc_step(int step_count, double step_max, int &status) {
+    float calc_step(int step_count, float step_max, int &status) {
         return type == 0 ? bracket(step_count, step_max, status) : backtrack(step_count, step_max, status);
     }
     long ls_cap() const { return std::max(1L, (long)inv_iteration * ls_step); }
-    void push_ls(double len, double val) {
+    void push_ls(float len, float val) {
         if ((size_t)ls_count >= ls_lens.size()) {
             ls_lens.resize(ls_count + 1);
             ls_vals.resize(ls_count + 1);
@@ -301,12 +319,14 @@ struct gb_optimizer {
     }
 
     // Optimizer::lineSearch (optimizer/optimizer.h:360-419)
-    int line_search(double f) {
+    // f: the misfit, a float in the reference (misfit->run)
+    int line_search(double f_run) {
+        const float f = (float)f_run;
         int status = 0;
-        double alpha = 0;
-        const double norm_m = amax(m_new), norm_p = amax(p_new);
-        const double gtg = dot(g_new, g_new), gtp = dot(g_new, p_new);
-        const double step_max = ls_step_max * norm_m / norm_p;
+        float alpha = 0;
+        const float norm_m = (float)amax(m_new), norm_p = (float)amax(p_new);
+        const float gtg = (float)dot(g_new, g_new), gtp = (float)dot(g_new, p_new);
+        const float step_max = ls_step_max * norm_m / norm_p;
         int step_count = 0;
         push_ls(0, f);
         if ((size_t)inv_count > ls_gtg.size()) {
@@ -315,7 +335,7 @@ struct gb_optimizer {
         }
         ls_gtg[inv_count - 1] = gtg;
         ls_gtp[inv_count - 1] = gtp;
-        double alpha_current = 0;
+        float alpha_current = 0;
         if (ls_step_init != 0 && ls_count <= 1)
             alpha = ls_step_init * norm_m / norm_p;
         else
@@ -330,15 +350,15 @@ struct gb_optimizer {
                 alpha_current = alpha;
                 const double v = evaluate(false, 0, alpha);
                 if (err) return -1;
-                push_ls(alpha, v);
+                push_ls(alpha, (float)v);
                 eval_count++;
                 step_count++;
                 alpha = calc_step(step_count, step_max, status);
                 std::cout << "  step " << (step_count < 10 ? "0" : "") << step_count
-                          << "  misfit = " << (float)(ls_vals[ls_count - 1] / ref) << std::endl;
+                          << "  misfit = " << ls_vals[ls_count - 1] / (float)ref << std::endl;
             }
             if (status > 0) {
-                std::cout << "  alpha = " << (float)alpha << std::endl;
+                std::cout << "  alpha = " << alpha << std::endl;
                 calc(m_new, 1, m_new, alpha - alpha_current, p_new);
                 return status;
             } else if (status < 0) {
@@ -349,7 +369,7 @@ struct gb_optimizer {
                 }
                 std::cout << "  restarting line search..." << std::endl;
                 restart_search();
-                return line_search(f);
+                return line_search(f_run);
             }
         }
     }
@@ -514,9 +534,9 @@ gb_optimizer *gb_optimizer_create(const gb_config *cfg, gb_solver *sol, gb_misfi
     o->inv_iteration = c.iv("inv_iteration");
     o->inv_cycle = c.iv("inv_cycle");
     o->ls_step = c.iv("ls_step");
-    o->ls_step_max = c.fv("ls_step_max");
-    o->ls_step_init = c.fv("ls_step_init");
-    o->ls_thresh = c.fv("ls_thresh");
+    o->ls_step_max = (float)c.fv("ls_step_max");
+    o->ls_step_init = (float)c.fv("ls_step_init");
+    o->ls_thresh = (float)c.fv("ls_thresh");
     o->nlcg_type = c.iv("nlcg_type");
     o->nlcg_thresh = c.fv("nlcg_thresh");
     o->lbfgs_mem = c.iv("lbfgs_mem");
@@ -568,6 +588,37 @@ int gb_optimizer_history(gb_optimizer *o, double *out, int n) {
     const int k = std::min<int>(n, (int)o->history.size());
     for (int i = 0; i < k && out; i++) out[i] = o->history[i];
     return (int)o->history.size();
+}
+
+double gb_linesearch_step(int optimizer, const double *lens, const double *vals, int ls_count, const double *gtg,
+                          const double *gtp, int inv_count, int step_count, int ls_step, double ls_thresh,
+                          double step_max, int *status) {
+    if (status) *status = -2;
+    if ((optimizer != 0 && optimizer != 1) || !lens || !vals || !gtg || !gtp || !status || step_count < 0 ||
+        ls_count < step_count + 1 || inv_count < 1 || !(ls_thresh > 1)) {
+        set_error("gb_linesearch_step: invalid history");
+        return 0;
+    }
+    gb_optimizer o;  // host state only: the step rule touches no device memory
+    o.type = optimizer;
+    o.ls_step = ls_step;
+    o.ls_thresh = (float)ls_thresh;
+    o.ls_lens.assign(lens, lens + ls_count);
+    o.ls_vals.assign(vals, vals + ls_count);
+    o.ls_count = ls_count;
+    o.ls_gtg.assign(gtg, gtg + inv_count);
+    o.ls_gtp.assign(gtp, gtp + inv_count);
+    o.inv_count = inv_count;
+    std::vector<float> x, f;
+    if (step_count == 0 && o.history_of(0, x, f) > 0 && inv_count < 2) {
+        // the rule then scales the previous iteration's step (optimizer.h:275-277)
+        set_error("gb_linesearch_step: an earlier iteration in the history needs inv_count >= 2");
+        return 0;
+    }
+    int st = 0;
+    const float a = o.calc_step(step_count, (float)step_max, st);
+    *status = st;
+    return a;
 }
 
 int gb_optimizer_evaluations(gb_optimizer *o, double *out, int n) {

@@ -23,11 +23,12 @@ arrays are the caller's, updated in place, as the reference aliases m_new
 and g_new to the solver's lambda/mu/rho and k_* (optimizer.h:498-503).
 
 Where the reference is undefined the oracle does what the GB300 optimizer
-does and counts the event in ``undefined_steps``: a fit whose curvature is
-not positive (goodEnough leaves bracket's alpha uninitialised; the fit is
-converted to float, optimizer.h:174-177, so p[0] underflows to 0 once steps
-reach ~1e20) ends the search at the best point evaluated; a search that has
-used the reference's inv_iteration * ls_step entries (optimizer.h:485-487,
+does and counts the event in ``undefined_steps``. goodEnough leaves
+bracket's alpha uninitialised when the fit, converted to float
+(optimizer.h:174-177), has no positive curvature: where only the conversion
+lost it (p[0] underflows once steps reach ~1e20) the double fit's minimum is
+taken, otherwise the search ends at the best point evaluated. A search that
+has used the reference's inv_iteration * ls_step entries (optimizer.h:485-487,
 written past after that) fails as one past ls_step does.
 """
 from __future__ import annotations
@@ -189,13 +190,17 @@ class Optimizer:
             return False, None
         idx = self.argmin(f, n) - 1
         fitlen = min(4, n - idx)
-        p = [F(v) for v in self.ops.polyfit(np.array(x[idx:idx + fitlen], np.float64),
-                                            np.array(f[idx:idx + fitlen], np.float64))]
-        if p[0] <= 0:
+        pd = self.ops.polyfit(np.array(x[idx:idx + fitlen], np.float64), np.array(f[idx:idx + fitlen], np.float64))
+        p = [F(v) for v in pd]
+        if p[0] > 0:
+            x0 = F(-p[1] / F(F(2) * p[0]))
+        elif pd[0] > 0:  # the float coefficient underflowed: the double fit's minimum
+            self.undefined_steps += 1
+            x0 = F(-pd[1] / (2 * pd[0]))
+        else:
             self.events.append("line search error")
             self.undefined_steps += 1
             return True, None
-        x0 = F(-p[1] / F(F(2) * p[0]))
         for i in range(1, n):
             if abs(F(np.log10(F(x[i] / x0)))) < thresh:
                 return True, x0
@@ -204,7 +209,11 @@ class Optimizer:
     @staticmethod
     def backtrack2(f0, g0, x1, f1, b1, b2):
         b1, b2 = F(b1), F(b2)
-        x2 = F(F(F(-g0 * x1) * x1) / F(F(2) * F(F(f1 - f0) - F(g0 * x1))))
+        # the slope is gtp/gtg, not gtp: with steps of ~1e20 the float
+        # numerator overflows to inf as the reference's does, and the clamp
+        # below then takes b2 * x1
+        with np.errstate(over="ignore", invalid="ignore"):
+            x2 = F(F(F(-g0 * x1) * x1) / F(F(2) * F(F(f1 - f0) - F(g0 * x1))))
         if x2 > F(b2 * x1):
             x2 = F(b2 * x1)
         elif x2 < F(b1 * x1):
