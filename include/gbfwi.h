@@ -118,6 +118,14 @@ int gb_export_model(gb_solver *s, int n);
 int gb_export_kernel(gb_solver *s, int n);
 /* Solver::exportTraces (solver/solver.h:38-108) of the last forward run. */
 int gb_export_traces(gb_solver *s, int isrc);
+/* The SU files alone, on the host (no device work): nrec traces of nt
+ * samples in host memory with Solver::exportTraces' 240-byte headers
+ * (solver/solver.h:38-108; source at xs, zs, receivers at rec_x, rec_z), and
+ * their reading as Misfit::importTraces (misfit/misfit.h:52-90), headers
+ * skipped. */
+int gb_su_write(const char *file, const float *traces, int nrec, int nt, float dt, float xs, float zs,
+                const float *rec_x, const float *rec_z);
+int gb_su_read(const char *file, float *traces, int nrec, int nt);
 
 /* Public device buffers (Solver's public members, solver/solver.h:122-156). */
 float *gb_solver_ptr(gb_solver *s, int which);

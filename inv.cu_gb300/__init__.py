@@ -98,6 +98,9 @@ def _declare(lib):
         "gb_export_model": (ctypes.c_int, [_vp, ctypes.c_int]),
         "gb_export_kernel": (ctypes.c_int, [_vp, ctypes.c_int]),
         "gb_export_traces": (ctypes.c_int, [_vp, ctypes.c_int]),
+        "gb_su_write": (ctypes.c_int, [ctypes.c_char_p, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                       ctypes.c_float, ctypes.c_float, _vp, _vp]),
+        "gb_su_read": (ctypes.c_int, [ctypes.c_char_p, _vp, ctypes.c_int, ctypes.c_int]),
         "gb_solver_ptr": (_vp, [_vp, ctypes.c_int]),
         "gb_solver_dims": (ctypes.c_int, [_vp] + [ctypes.POINTER(ctypes.c_int)] * 5),
         "gb_solver_steps": (ctypes.c_int, [_vp] + [_fp] * 3),
@@ -507,6 +510,23 @@ class Misfit:
 
     def __del__(self):
         self.close()
+
+
+def su_write(path: str, traces, dt: float, xs: float, zs: float, rec_x, rec_z) -> None:
+    """An SU file as Solver::exportTraces writes it (solver/solver.h:38-108);
+    traces [nrec, nt] in host memory."""
+    t = np.ascontiguousarray(traces, dtype=np.float32)
+    rx, rz = _f32(rec_x), _f32(rec_z)
+    nrec, nt = t.shape
+    check(lib().gb_su_write(path.encode(), t.ctypes.data_as(_vp), nrec, nt, float(dt), float(xs), float(zs),
+                            rx.ctypes.data_as(_vp), rz.ctypes.data_as(_vp)), "su_write")
+
+
+def su_read(path: str, nrec: int, nt: int) -> np.ndarray:
+    """Traces [nrec, nt] of an SU file as Misfit::importTraces reads them."""
+    out = np.zeros((nrec, nt), np.float32)
+    check(lib().gb_su_read(path.encode(), out.ctypes.data_as(_vp), nrec, nt), "su_read")
+    return out
 
 
 def linesearch_step(optimizer: int, lens, vals, gtg, gtp, step_count: int, ls_step: int, ls_thresh: float,

@@ -217,6 +217,23 @@ int gb_export_traces(gb_solver *s, int isrc) {
     return GB_OK;
 }
 
+int gb_su_write(const char *file, const float *traces, int nrec, int nt, float dt, float xs, float zs,
+                const float *rec_x, const float *rec_z) {
+    if (!file || !traces || !rec_x || !rec_z || nrec < 1 || nt < 1) {
+        set_error("gb_su_write: bad arguments");
+        return GB_ERR_ARG;
+    }
+    return write_su(file, traces, nrec, nt, dt, xs, zs, rec_x, rec_z);
+}
+
+int gb_su_read(const char *file, float *traces, int nrec, int nt) {
+    if (!file || !traces || nrec < 1 || nt < 1) {
+        set_error("gb_su_read: bad arguments");
+        return GB_ERR_ARG;
+    }
+    return read_su(file, traces, nrec, nt);
+}
+
 float *gb_slot_ptr(gb_solver *s, int slot, int which) {
     if (!s) return nullptr;
     Solver &v = s->s;
