@@ -85,6 +85,10 @@ typedef struct gb_solver gb_solver;
 /* Solver::init + FdmSolver::init (solver/solver.h:158-224,
  * solver/fdm.h:350-462): grid inferred from model_true/proc000000_{x,z}.bin. */
 gb_solver *gb_solver_create(const gb_config *cfg);
+/* The grid gb_solver_create infers, on the host (no device work): nx, nz,
+ * xmax, zmax and the point count from <dir>/model_true/proc000000_{x,z}.bin
+ * as FdmSolver::init does (solver/fdm.h:354-391). */
+int gb_infer_grid(const char *dir, int *nx, int *nz, float *xmax, float *zmax, int *npt);
 /* Same, with the grid given instead of read from model files:
  * dx = xmax/(nx-1), dz = zmax/(nz-1). */
 gb_solver *gb_solver_create_grid(const gb_config *cfg, int nx, int nz, float xmax, float zmax);

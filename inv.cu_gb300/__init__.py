@@ -98,6 +98,9 @@ def _declare(lib):
         "gb_export_model": (ctypes.c_int, [_vp, ctypes.c_int]),
         "gb_export_kernel": (ctypes.c_int, [_vp, ctypes.c_int]),
         "gb_export_traces": (ctypes.c_int, [_vp, ctypes.c_int]),
+        "gb_infer_grid": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                         ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
+                                         ctypes.POINTER(ctypes.c_int)]),
         "gb_su_write": (ctypes.c_int, [ctypes.c_char_p, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_float,
                                        ctypes.c_float, ctypes.c_float, _vp, _vp]),
         "gb_su_read": (ctypes.c_int, [ctypes.c_char_p, _vp, ctypes.c_int, ctypes.c_int]),
@@ -510,6 +513,16 @@ class Misfit:
 
     def __del__(self):
         self.close()
+
+
+def infer_grid(directory: str):
+    """(nx, nz, xmax, zmax, npt) of <directory>/model_true, as FdmSolver::init
+    infers them (solver/fdm.h:354-391)."""
+    nx, nz, npt = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    xm, zm = ctypes.c_float(), ctypes.c_float()
+    check(lib().gb_infer_grid(directory.encode(), ctypes.byref(nx), ctypes.byref(nz), ctypes.byref(xm),
+                              ctypes.byref(zm), ctypes.byref(npt)), "infer_grid")
+    return nx.value, nz.value, xm.value, zm.value, npt.value
 
 
 def su_write(path: str, traces, dt: float, xs: float, zs: float, rec_x, rec_z) -> None:

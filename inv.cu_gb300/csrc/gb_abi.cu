@@ -66,6 +66,14 @@ gb_solver *make_solver(const gb_config *cfg, int nx, int nz, float xmax, float z
 
 extern "C" {
 
+int gb_infer_grid(const char *dir, int *nx, int *nz, float *xmax, float *zmax, int *npt) {
+    if (!dir || !nx || !nz || !xmax || !zmax || !npt) {
+        set_error("gb_infer_grid: null argument");
+        return GB_ERR_ARG;
+    }
+    return infer_grid(dir, nx, nz, xmax, zmax, npt);
+}
+
 gb_solver *gb_solver_create(const gb_config *cfg) {
     if (!cfg) {
         set_error("gb_solver_create: null config");
