@@ -541,6 +541,12 @@ gb_optimizer *gb_optimizer_create(const gb_config *cfg, gb_solver *sol, gb_misfi
     o->nlcg_thresh = c.fv("nlcg_thresh");
     o->lbfgs_mem = c.iv("lbfgs_mem");
     o->lbfgs_thresh = c.fv("lbfgs_thresh");
+    if (o->type == 1 && o->lbfgs_mem < 1) {
+        // the reference indexes lbfgs_S[lbfgs_mem - 1] (optimizer/lbfgs.h:29)
+        set_error("gb_optimizer_create: lbfgs_mem must be at least 1 for L-BFGS");
+        delete o;
+        return nullptr;
+    }
     o->ls_lens.resize(std::max(1, o->inv_iteration * o->ls_step));
     o->ls_vals.resize(o->ls_lens.size());
     o->ls_gtg.resize(std::max(1, o->inv_iteration));

@@ -166,3 +166,17 @@ def test_mesh2grid_fast_path_matches_brute_force(gpu, orc):
     lam, mu = orc.vps2lm(lam, mu, r)
     np.testing.assert_array_equal(got["rho"], r)
     assert cases.rel(got["lambda"], lam) < 1e-6 and cases.rel(got["mu"], mu) < 1e-6
+
+
+def test_lbfgs_without_memory_is_rejected(gpu, tmp_path):
+    """optimizer = 1 with lbfgs_mem 0 (the reference indexes lbfgs_S[-1])
+    fails at creation instead of running a search with no history buffers."""
+    case = cases.make_case(wave="sh", nx=40, nz=30, nt=20, nsrc=1, nrec=4)
+    cfg, sol = cases.gpu_solver(gpu, case, directory=str(tmp_path))
+    cfg.set("optimizer", 1)
+    cfg.set("lbfgs_mem", 0)
+    mis = gpu.Misfit.from_obs(0, sol, {"y": np.zeros((1, 4, 20), np.float32)})
+    with pytest.raises(gpu.GbError, match="lbfgs_mem"):
+        gpu.Optimizer(cfg, sol, mis)
+    mis.close()
+    sol.close()
