@@ -29,3 +29,16 @@ def test_mode_without_a_case_does_nothing(pkg, tmp_path):
     assert r.stdout == "" and r.stderr == ""
     # the config load itself creates output/, empty (lib/config.h:101-104)
     assert (tmp_path / "output").is_dir() and not any((tmp_path / "output").iterdir())
+
+
+def test_clean_flag_empties_output(pkg, tmp_path):
+    """clean = 1 removes output/ before it is made again; clean = 0 keeps
+    what is there (lib/config.h:101-104)."""
+    (tmp_path / "output").mkdir()
+    (tmp_path / "output" / "keep.bin").write_bytes(b"x")
+    (tmp_path / "config.ini").write_text("[global]\nmode = 9\nclean = 0\n")
+    assert run(pkg, [str(tmp_path)], str(tmp_path)).returncode == 0
+    assert (tmp_path / "output" / "keep.bin").exists()
+    (tmp_path / "config.ini").write_text("[global]\nmode = 9\nclean = 1\n")
+    assert run(pkg, [str(tmp_path)], str(tmp_path)).returncode == 0
+    assert (tmp_path / "output").is_dir() and not any((tmp_path / "output").iterdir())
