@@ -16,7 +16,9 @@ timed with CUDA events on the solver's stream; `e2e` is the same metric
 through the C ABI from pinned host buffers (model and observed traces in,
 kernels and misfit out, copies inside the timed region). The reference arm
 times the CPU port of the reference algorithm (oracle/, OpenMP on all host
-cores) on a bounded sample of the same workload.
+cores), one full shot per step, and beside it one full gradient through the
+reference's own CUDA kernels on the GPU (`reference_gpu`, also in the main
+line). Both arms print the same `config`.
 """
 from __future__ import annotations
 
@@ -105,7 +107,7 @@ CONFIG_DESC = {
                 "envelope misfit, Gaussian smoothing sigma 5, checkpoints every 10 steps",
     "grid": [NX, NZ], "nt": NT, "shots": NSHOT, "receivers": NX, "source_receiver_depth_m": 2 * H,
     "sfe": SFE, "misfit": "envelope",
-    "filter_sigma": SIGMA, "step": "one gradient: 16 forward + envelope misfit + 16 adjoint + smoothing",
+    "filter_sigma": SIGMA,
     "l2": "flushed (256 MB write) between timed steps; each step also streams 3.1 GB of checkpoints",
 }
 
@@ -194,48 +196,110 @@ def profiled_traffic(kernel_tag):
 
 
 # ----------------------------------------------------------------------------
-# CPU port of the reference (oracle), bounded sample
+# Baseline legs: the CPU port of the reference (oracle/, OpenMP) and the
+# reference's own CUDA kernels (oracle/_ref, driven by oracle/ref_harness.cu
+# in the reference's launch shapes and host loop). Checkers and baselines
+# only: neither is on the product path.
 # ----------------------------------------------------------------------------
-def cpu_sample(wl, nshots=1):
-    """Times the oracle (C restatement of the reference, OpenMP over all host
-    cores) on `nshots` full shots of the workload: forward with checkpoints,
-    envelope misfit, adjoint; plus one smoothing of the three kernels.
-    Returns (seconds per 16-shot gradient, threads, description)."""
+def _oracle_problem(wl):
     from oracle import oracle as orc
 
-    orc.set_threads(os.cpu_count() or 1)
-    threads = orc.num_threads()
     lam, mu, rho = wl["init"]
     v = wl["values"]
-    nt = NT
     src = np.array(wl["src"], np.float32)
     rec = np.array(wl["rec"], np.float32)
-    stf = [np.zeros(len(src) * nt, np.float32) for _ in range(3)]
+    stf = [np.zeros(len(src) * NT, np.float32) for _ in range(3)]
     for s in range(len(src)):
-        c = orc.ricker(nt, DT, *src[s, 3:7])
+        c = orc.ricker(NT, DT, *src[s, 3:7])
         for q in range(3):
-            stf[q][s * nt:(s + 1) * nt] = c[q]
+            stf[q][s * NT:(s + 1) * NT] = c[q]
     ab = orc.absbound(NX, NZ, v["abs_width"], v["abs_alpha"], 1, 1, 1, 0)
     dx = float(np.float32(wl["xmax"]) / np.float32(NX - 1))
-    pb = orc.Problem(nx=NX, nz=NZ, nt=nt, dx=dx, dz=dx, dt=DT, sh=True, psv=False, sfe=SFE, lam=lam, mu=mu,
-                     rho=rho, ab=ab, stf=tuple(stf),
-                     src_id=(orc.calc_idx(src[:, 0], wl["xmax"], NX), orc.calc_idx(src[:, 1], wl["zmax"], NZ)),
-                     rec_id=(orc.calc_idx(rec[:, 0], wl["xmax"], NX), orc.calc_idx(rec[:, 1], wl["zmax"], NZ)),
-                     inv_lambda=False, inv_mu=True, inv_rho=True)
+    return orc.Problem(nx=NX, nz=NZ, nt=NT, dx=dx, dz=dx, dt=DT, sh=True, psv=False, sfe=SFE, lam=lam, mu=mu,
+                       rho=rho, ab=ab, stf=tuple(stf),
+                       src_id=(orc.calc_idx(src[:, 0], wl["xmax"], NX), orc.calc_idx(src[:, 1], wl["zmax"], NZ)),
+                       rec_id=(orc.calc_idx(rec[:, 0], wl["xmax"], NX), orc.calc_idx(rec[:, 1], wl["zmax"], NZ)),
+                       inv_lambda=False, inv_mu=True, inv_rho=True)
+
+
+class CpuPort:
+    """The oracle (C restatement of the reference, OpenMP over all host cores)
+    on the workload. One step of it is one full shot: forward with
+    checkpoints, envelope misfit against 0.9 x the synthetics, adjoint with
+    kernel accumulation. The smoothing of the three kernels (once per
+    gradient) is timed on its own; a gradient is 16 shots + one smoothing."""
+
+    def __init__(self, wl):
+        from oracle import oracle as orc
+
+        self.orc = orc
+        orc.set_threads(os.cpu_count() or 1)
+        self.threads = orc.num_threads()
+        self.pb = _oracle_problem(wl)
+        self.kern = None
+
+    def shot(self, s):
+        orc = self.orc
+        t0 = time.perf_counter()
+        _, oy, _, ck = orc.forward(self.pb, s % NSHOT, adj=True)
+        _, ad = orc.envelope_misfit(oy, oy * np.float32(0.9), DT)
+        self.kern = orc.adjoint(self.pb, [np.zeros_like(ad), ad, np.zeros_like(ad)], ck, self.kern)
+        return time.perf_counter() - t0
+
+    def smoothing(self):
+        t0 = time.perf_counter()
+        for k in self.kern:
+            self.orc.gaussian_filter(NX, NZ, SIGMA, k)
+        return time.perf_counter() - t0
+
+
+def cpu_sample(wl, nshots=1):
+    """Bounded CPU sample beside the GPU number: `nshots` full shots and one
+    smoothing. Returns (seconds per 16-shot gradient, threads, description)."""
+    port = CpuPort(wl)
+    t_shot = sum(port.shot(s) for s in range(nshots)) / nshots
+    t_filter = port.smoothing()
+    desc = ("%d of %d shots at full size (forward %d steps with checkpoints, envelope misfit, adjoint) plus "
+            "one smoothing of 3 kernels; per-gradient time = 16 x shot + smoothing" % (nshots, NSHOT, NT))
+    return NSHOT * t_shot + t_filter, port.threads, desc
+
+
+def reference_gpu_sample(wl):
+    """One full 16-shot gradient through the reference's own CUDA kernels
+    (compiled from its sources for sm_103a), in its launch shapes (nx blocks
+    of nz threads, six launches per time step, one-thread-block source and
+    receiver launches) and host loop (solver/fdm.h:515-612: checkpoints
+    copied to pageable host memory and back with blocking copies; per-trace
+    envelope misfit with cuFFT and cuBLAS, misfit/envelope.h:58-90), plus the
+    smoothing of the three kernels with its filter kernels. Wall time around
+    the whole gradient (the reference's host loop is synchronous). Returns a
+    dict for the JSON line, or one that says why it did not run."""
+    from oracle import oracle as orc
+
+    if not orc.ref_available():
+        return {"unavailable": "the reference's kernels were not built (oracle/_ref/inv_ref.cubin absent)"}
+    pb = _oracle_problem(wl)
+    # warm-up: module load, cuFFT/cuBLAS handles, first launches (one short shot)
+    short = _oracle_problem(wl)
+    short.nt = 200
+    short.stf = tuple(np.ascontiguousarray(a.reshape(NSHOT, NT)[:, :200]).ravel() for a in pb.stf)
+    _, oy, _, ck = orc.ref_forward(short, 0, adj=True)
+    _, ad = orc.ref_misfit(1, oy, oy * np.float32(0.9), DT)
+    orc.ref_adjoint(short, [np.zeros_like(ad), ad, np.zeros_like(ad)], ck)
     t0 = time.perf_counter()
     kern = None
-    for s in range(nshots):
-        _, oy, _, ck = orc.forward(pb, s, adj=True)
-        _, ad = orc.envelope_misfit(oy, oy * np.float32(0.9), DT)
-        kern = orc.adjoint(pb, [np.zeros_like(ad), ad, np.zeros_like(ad)], ck, kern)
-    t_shot = (time.perf_counter() - t0) / nshots
-    t1 = time.perf_counter()
+    for s in range(NSHOT):
+        _, oy, _, ck = orc.ref_forward(pb, s, adj=True)
+        _, ad = orc.ref_misfit(1, oy, oy * np.float32(0.9), DT)
+        kern = orc.ref_adjoint(pb, [np.zeros_like(ad), ad, np.zeros_like(ad)], ck, kern)
     for k in kern:
-        orc.gaussian_filter(NX, NZ, SIGMA, k)
-    t_filter = time.perf_counter() - t1
-    desc = ("%d of %d shots at full size (forward %d steps with checkpoints, envelope misfit, adjoint) plus "
-            "one smoothing of 3 kernels; per-gradient time = 16 x shot + smoothing" % (nshots, NSHOT, nt))
-    return NSHOT * t_shot + t_filter, threads, desc
+        orc.ref_gaussian(NX, NZ, SIGMA, k)
+    t = time.perf_counter() - t0
+    return {"value": round(NSHOT / t, 3), "unit": "shots/s", "ms_per_gradient": round(1e3 * t, 1),
+            "sample": "one full 16-shot gradient, wall time (no extrapolation)",
+            "what": "the reference's own kernels compiled from its sources for sm_103a, run in its launch shapes "
+                    "and host loop: six launches per step, checkpoints to pageable host memory by blocking "
+                    "copies, per-trace cuFFT/cuBLAS envelope misfit, its Gaussian filter"}
 
 
 # ----------------------------------------------------------------------------
@@ -355,6 +419,12 @@ def run_ours(args, ws, rank, local):
         mp.close()
         sp.close()
 
+    ref_gpu = None
+    if rank == 0 and ws == 1 and not args.no_ref_gpu:
+        ref_gpu = _reference_gpu_leg(wl)
+        if "value" in ref_gpu:
+            ref_gpu["ours_over_reference"] = round(value / ref_gpu["value"], 2)
+            ref_gpu["ours_e2e_over_reference"] = round(e2e["value"] / ref_gpu["value"], 2)
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         t_grad, threads, desc = cpu_sample(wl)
@@ -366,10 +436,13 @@ def run_ours(args, ws, rank, local):
         "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded faulted layered model with the workload's shapes; no dataset)",
-        "config": dict(CONFIG_DESC, batch=st.batch_capacity, tile=[st.tile_tz, st.tile_tx],
-                       ckpt="fp32", parallelism="shots sharded over %d rank(s), replicas" % ws),
+        "config": dict(CONFIG_DESC),
+        "run": {"step": "one gradient: 16 forward + envelope misfit + 16 adjoint + smoothing",
+                "batch": st.batch_capacity, "tile": [st.tile_tz, st.tile_tx], "ckpt": "fp32",
+                "parallelism": "shots sharded over %d rank(s), replicas" % ws},
         "cell_updates_per_s": round(2.0 * cells * NT * NSHOT * args.steps * ws / (total_ms / 1e3), 1),
         "misfit": mis_val, "plain_path": plain, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+        "reference_gpu": ref_gpu,
         "breakdown_ms_per_gradient": {k: round(getattr(st, k) / args.steps, 3)
                                       for k in ("forward_ms", "adjoint_ms", "misfit_ms", "filter_ms")},
         "gpu_launches": int(st.launches), "clocks": clocks,
@@ -656,29 +729,54 @@ def run_profile_case(args):
 
 
 def run_reference(args, ws, rank):
+    """The reference arm. The reference's path is CUDA only; its CPU
+    restatement (oracle/, pinned against the reference's golden seismograms)
+    is the CPU implementation timed here, on all host cores: --warmup shots,
+    then --steps timed shots (one shot per step, shots 0..15 in turn), and
+    one smoothing of the three kernels timed on its own; shots/s counts a
+    gradient as 16 shots + one smoothing. Beside it, when a GPU and the
+    reference's compiled kernels are present, one full gradient through
+    those kernels (`reference_gpu`)."""
     if rank != 0:
         return
     wl = workload()
-    samples = []
-    threads, desc = 0, ""
-    for q in range(args.warmup + args.steps):
-        t_grad, threads, desc = cpu_sample(wl)
-        if q >= args.warmup:
-            samples.append(t_grad)
-    value = NSHOT / (sum(samples) / len(samples))
+    port = CpuPort(wl)
+    for q in range(args.warmup):
+        port.shot(q)
+    shots = [port.shot(args.warmup + q) for q in range(args.steps)]
+    t_smooth = port.smoothing()
+    t_shot = sum(shots) / len(shots)
+    value = NSHOT / (NSHOT * t_shot + t_smooth)
+    ms_step = 1e3 * (t_shot + t_smooth / NSHOT)
+    desc = ("one full shot per step (forward %d steps with checkpoints, envelope misfit, adjoint), %d steps; "
+            "smoothing of 3 kernels timed once and shared over 16 shots" % (NT, args.steps))
     line = {
         "metric": METRIC, "value": round(value, 4), "unit": "shots/s", "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": round(1e3 * sum(samples) / len(samples), 1),
+        "warmup": args.warmup, "ms_per_step": round(ms_step, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded faulted layered model with the workload's shapes; no dataset)",
-        "config": dict(CONFIG_DESC, parallelism="host cores"), "impl": "reference",
-        "cpu_baseline": {"value": round(value, 4), "unit": "shots/s", "cores": threads, "kind": "port",
+        "config": dict(CONFIG_DESC), "impl": "reference",
+        "cpu_baseline": {"value": round(value, 4), "unit": "shots/s", "cores": port.threads, "kind": "port",
                          "sample": desc},
         "e2e": {"value": round(value, 4), "unit": "shots/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "run": {"parallelism": "host cores (OpenMP over columns)", "step": "one shot"},
         "note": "the reference's path is CUDA only; its CPU restatement (oracle/, pinned against the "
                 "reference's golden seismograms) is the CPU implementation timed here",
     }
+    if not args.no_ref_gpu:
+        line["reference_gpu"] = _reference_gpu_leg(wl)
     print(json.dumps(line), flush=True)
+
+
+def _reference_gpu_leg(wl):
+    try:
+        import __graft_entry__ as ge
+
+        if ge.load_package().device_count() < 1:
+            return {"unavailable": "no CUDA device"}
+        return reference_gpu_sample(wl)
+    except Exception as e:  # reported in the line, never fatal to the arm
+        return {"unavailable": "%s: %s" % (type(e).__name__, e)}
 
 
 # ----------------------------------------------------------------------------
@@ -711,6 +809,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-path leg")
+    ap.add_argument("--no-ref-gpu", action="store_true", help="skip the reference-kernels-on-GPU leg")
     ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
                     help="c2 is the headline; the others print their own line")
     ap.add_argument("--shots", type=int, default=0, help="shot count for c3/c5 (default 64/16)")

@@ -206,21 +206,24 @@ gb_filter *gb_filter_create(int nx, int nz, int sigma);
 int gb_filter_apply(gb_filter *f, float *d_data);
 void gb_filter_destroy(gb_filter *f);
 
-/* Allocation-free Gaussian smoothing. No counterpart in the reference: it is
- * an addition for callers that cannot allocate device memory at the time of
- * the call, such as code running between the steps of a captured CUDA graph
- * or under an allocator owned by another runtime (a host application that
- * hands over one pre-sized buffer and forbids further cudaMalloc). It gives
- * the same result as gb_filter_create + gb_filter_apply on d_data
- * (float[nx*nz] on the current device) but keeps its scratch in a fixed
- * array inside the library: nx*nz <= GB_NOALLOC_MAX_CELLS and
- * max(nx, nz) <= GB_NOALLOC_MAX_SIDE, else GB_ERR_ARG. That array (about
- * 16.1 MB) stays reserved on every device that loads the library until the
- * process exits. The first call on a device looks up the array's address;
- * make that first call before any stream capture. All calls share the one
- * array, so calls that overlap on the GPU (from several host threads or
- * streams) race; this call runs on the legacy default stream and returns
- * after the work is done. */
+/* Allocation-free Gaussian smoothing. No counterpart in the reference: an
+ * addition for callers that cannot allocate device memory when they smooth a
+ * gradient. Two kinds of caller need it: a host application that hands all
+ * device memory to its own pool allocator and lets no library call
+ * cudaMalloc (a second allocator would fragment or overrun the pool), and a
+ * caller that keeps other streams busy and cannot take the device-wide
+ * synchronisation that cudaMalloc/cudaFree may imply. It gives the same
+ * result as gb_filter_create + gb_filter_apply on d_data (float[nx*nz] on the
+ * current device): the same kernels sum the same terms in the same order.
+ * Its scratch is a fixed array inside the library, so the grid is limited:
+ * nx*nz <= GB_NOALLOC_MAX_CELLS and max(nx, nz) <= GB_NOALLOC_MAX_SIDE, else
+ * GB_ERR_ARG. That array (about 16.1 MB) stays reserved on every device that
+ * loads the library until the process exits. The first call on a device looks
+ * up the array's device address (with that device current); make that first
+ * call before any stream capture. Every call on a device shares that
+ * device's one array and leaves its contents behind, so calls that overlap
+ * on the GPU (several host threads calling at once) race. The call launches
+ * on the legacy default stream and returns once its kernels have finished. */
 #define GB_NOALLOC_MAX_CELLS 4194304
 #define GB_NOALLOC_MAX_SIDE 8192
 int gb_filter_apply_noalloc(int nx, int nz, int sigma, float *d_data);

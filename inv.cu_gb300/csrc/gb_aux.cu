@@ -209,10 +209,27 @@ __global__ void k_gauss_weights(float *w, int m, int sigma) {
     w[x] = (1 / (sqrtf(2 * pi) * sigmaf)) * expf(-xf * xf / (2 * sigmaf * sigmaf));
 }
 
+// The cutoff m = 1 + the index of the last nonzero weight (at least 1): the
+// value gb_filter_create reads back to the host, here written to device
+// memory for the allocation-free path.
+__global__ void k_gauss_cutoff(const float *w, int len, int *m_out) {
+    __shared__ int last;
+    if (threadIdx.x == 0) last = 1;
+    __syncthreads();
+    for (int x = threadIdx.x; x < len; x += blockDim.x)
+        if (w[x] != 0.f) atomicMax(&last, x + 1);
+    __syncthreads();
+    if (threadIdx.x == 0) *m_out = last;
+}
+
+// The filter kernels below take the cutoff m by value, or from device memory
+// when m_dev is not null.
+
 // Partial sums S(i) = sum_{n=0}^{i} g(i-n), added in ascending n.
-__global__ void k_gauss_norm(const float *w, int m, float *s, int len) {
+__global__ void k_gauss_norm(const float *w, int m, float *s, int len, const int *m_dev) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= len) return;
+    if (m_dev) m = *m_dev;
     float acc = 0.f;
     for (int n = max(0, i - m + 1); n <= i; n++) acc += w[i - n];
     s[i] = acc;
@@ -221,9 +238,10 @@ __global__ void k_gauss_norm(const float *w, int m, float *s, int len) {
 // X pass: tmp[i,j] = sum_n g(i-n) data[n,j]; thread per cell, consecutive
 // threads along z (coalesced).
 __global__ void k_gauss_x(const float *__restrict__ data, float *__restrict__ tmp, const float *__restrict__ w, int m,
-                          int nx, int nz) {
+                          int nx, int nz, const int *m_dev) {
     const size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (k >= (size_t)nx * nz) return;
+    if (m_dev) m = *m_dev;
     const int i = (int)(k / nz), j = (int)(k - (size_t)i * nz);
     float acc = 0.f;
     for (int n = max(0, i - m + 1); n <= i; n++) acc = fmaf(__ldg(w + i - n), __ldg(data + (size_t)n * nz + j), acc);
@@ -232,9 +250,11 @@ __global__ void k_gauss_x(const float *__restrict__ data, float *__restrict__ tm
 
 // Z pass with the normalisation.
 __global__ void k_gauss_z(float *__restrict__ data, const float *__restrict__ tmp, const float *__restrict__ w, int m,
-                          const float *__restrict__ sx, const float *__restrict__ sz, int nx, int nz) {
+                          const float *__restrict__ sx, const float *__restrict__ sz, int nx, int nz,
+                          const int *m_dev) {
     const size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (k >= (size_t)nx * nz) return;
+    if (m_dev) m = *m_dev;
     const int i = (int)(k / nz), j = (int)(k - (size_t)i * nz);
     const float *row = tmp + (size_t)i * nz;
     float acc = 0.f;
@@ -284,8 +304,8 @@ gb_filter *gb_filter_create(int nx, int nz, int sigma) {
     int m = len;
     while (m > 1 && hw[m - 1] == 0.f) m--;
     f->m = m;
-    gb::k_gauss_norm<<<(nx + 255) / 256, 256, 0, f->st>>>(f->w, m, f->sx, nx);
-    gb::k_gauss_norm<<<(nz + 255) / 256, 256, 0, f->st>>>(f->w, m, f->sz, nz);
+    gb::k_gauss_norm<<<(nx + 255) / 256, 256, 0, f->st>>>(f->w, m, f->sx, nx, nullptr);
+    gb::k_gauss_norm<<<(nz + 255) / 256, 256, 0, f->st>>>(f->w, m, f->sz, nz, nullptr);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(f->st);
     if (e != cudaSuccess) {
@@ -303,8 +323,8 @@ int gb_filter_apply(gb_filter *f, float *d_data) {
     }
     const size_t n = (size_t)f->nx * f->nz;
     const unsigned blocks = (unsigned)((n + 255) / 256);
-    gb::k_gauss_x<<<blocks, 256, 0, f->st>>>(d_data, f->tmp, f->w, f->m, f->nx, f->nz);
-    gb::k_gauss_z<<<blocks, 256, 0, f->st>>>(d_data, f->tmp, f->w, f->m, f->sx, f->sz, f->nx, f->nz);
+    gb::k_gauss_x<<<blocks, 256, 0, f->st>>>(d_data, f->tmp, f->w, f->m, f->nx, f->nz, nullptr);
+    gb::k_gauss_z<<<blocks, 256, 0, f->st>>>(d_data, f->tmp, f->w, f->m, f->sx, f->sz, f->nx, f->nz, nullptr);
     GB_CUDA_TRY(cudaGetLastError());
     GB_CUDA_TRY(cudaStreamSynchronize(f->st));
     return GB_OK;
@@ -325,19 +345,22 @@ void gb_filter_destroy(gb_filter *f) {
 // without allocation (gb_filter_apply_noalloc)
 namespace {
 
-// Scratch of the allocation-free filter: the x-pass result and the weights
-// and partial-sum profiles. Reserved on every device that loads the library
-// for the life of the process (16 MiB + 96 KiB). Calls overwrite every
-// element they read, so nothing needs clearing between calls.
+// Scratch of the allocation-free filter: the x-pass result, the weights,
+// the partial-sum profiles and the weight cutoff. Reserved on every device
+// that loads the library for the life of the process (16 MiB + 96 KiB).
+// Every call writes each element it later reads (the cutoff included) before
+// reading it, so nothing needs clearing between calls.
 static __device__ __align__(256) float g_na_tmp[GB_NOALLOC_MAX_CELLS];
 static __device__ __align__(256) float g_na_w[GB_NOALLOC_MAX_SIDE];
 static __device__ __align__(256) float g_na_sx[GB_NOALLOC_MAX_SIDE];
 static __device__ __align__(256) float g_na_sz[GB_NOALLOC_MAX_SIDE];
+static __device__ __align__(256) int g_na_m[1];
 
 // Device addresses of the arrays above, looked up once per device. In host
 // code the array names are host-side stand-ins, never device addresses.
 struct NoAllocAddr {
     float *tmp = nullptr, *w = nullptr, *sx = nullptr, *sz = nullptr;
+    int *m = nullptr;
     bool ready = false;
 };
 constexpr int kNoAllocDevices = 64;
@@ -358,6 +381,7 @@ int noalloc_addresses(NoAllocAddr *out) {
         GB_CUDA_TRY(cudaGetSymbolAddress((void **)&a.w, g_na_w));
         GB_CUDA_TRY(cudaGetSymbolAddress((void **)&a.sx, g_na_sx));
         GB_CUDA_TRY(cudaGetSymbolAddress((void **)&a.sz, g_na_sz));
+        GB_CUDA_TRY(cudaGetSymbolAddress((void **)&a.m, g_na_m));
         a.ready = true;
     }
     *out = a;
@@ -382,17 +406,17 @@ extern "C" int gb_filter_apply_noalloc(int nx, int nz, int sigma, float *d_data)
     int rc = noalloc_addresses(&a);
     if (rc) return rc;
     const int len = std::max(nx, nz);
-    // Weights at distance >= 16 sigma are below 1e-55 and come out of expf
-    // as exactly 0, so summing from there (instead of from the last nonzero
-    // weight, which gb_filter_create reads back) adds only exact zeros.
-    const int m = std::min(len, (int)std::ceil(16.0 * sigma) + 2);
     const size_t n = (size_t)nx * nz;
     const unsigned blocks = (unsigned)((n + 255) / 256);
+    // The weights, then the cutoff gb_filter_create uses (the last nonzero
+    // weight), found on the device and read there by the filter kernels, so
+    // both entry points sum exactly the same terms.
     gb::k_gauss_weights<<<(len + 255) / 256, 256>>>(a.w, len, sigma);
-    gb::k_gauss_norm<<<(nx + 255) / 256, 256>>>(a.w, m, a.sx, nx);
-    gb::k_gauss_norm<<<(nz + 255) / 256, 256>>>(a.w, m, a.sz, nz);
-    gb::k_gauss_x<<<blocks, 256>>>(d_data, a.tmp, a.w, m, nx, nz);
-    gb::k_gauss_z<<<blocks, 256>>>(d_data, a.tmp, a.w, m, a.sx, a.sz, nx, nz);
+    gb::k_gauss_cutoff<<<1, 256>>>(a.w, len, a.m);
+    gb::k_gauss_norm<<<(nx + 255) / 256, 256>>>(a.w, len, a.sx, nx, a.m);
+    gb::k_gauss_norm<<<(nz + 255) / 256, 256>>>(a.w, len, a.sz, nz, a.m);
+    gb::k_gauss_x<<<blocks, 256>>>(d_data, a.tmp, a.w, len, nx, nz, a.m);
+    gb::k_gauss_z<<<blocks, 256>>>(d_data, a.tmp, a.w, len, a.sx, a.sz, nx, nz, a.m);
     GB_CUDA_TRY(cudaGetLastError());
     GB_CUDA_TRY(cudaStreamSynchronize(0));
     return GB_OK;

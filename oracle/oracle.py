@@ -48,16 +48,18 @@ class OrcParams(ctypes.Structure):
     ]
 
 
-REF_SRC = os.environ.get("GBFWI_REF_SRC", "/root/reference")
+# checkout of the reference sources, named by the environment (GBFWI_REF_SRC)
+REF_SRC = os.environ.get("GBFWI_REF_SRC", "")
 REF_CUBIN = os.path.join(_HERE, "_ref", "inv_ref.cubin")
 _REF = None
 
 
 def build() -> str:
     """Compile the C oracle (gcc) and the reference-kernel harness (nvcc) with
-    the Makefile, and the reference's kernels where its sources are present."""
+    the Makefile, and the reference's kernels when GBFWI_REF_SRC names a
+    checkout of its sources (the cubin built earlier is kept otherwise)."""
     subprocess.run(["make", "-s", "-C", _HERE, "all", "harness"], check=True)
-    if os.path.exists(os.path.join(REF_SRC, "inv.cu")):
+    if REF_SRC and os.path.exists(os.path.join(REF_SRC, "inv.cu")):
         subprocess.run(["make", "-s", "-C", _HERE, "ref", "REFSRC=" + REF_SRC], check=True)
     return os.path.join(_HERE, "_build", "liboracle.so")
 

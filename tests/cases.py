@@ -54,6 +54,29 @@ def make_case(wave="psv", nx=120, nz=100, nt=600, nsrc=2, nrec=40, sfe=10, seed=
                 values=values, src=src, rec=rec, vp=vp, vs=vs, rho=rho, dt=dt)
 
 
+def checkerboard_case(nt=2000, nsrc=4):
+    """The 200 x 200 P-SV checkerboard at 10 m, dt 1 ms: vp 3000, vs 1732,
+    rho 2600 with a +-5 % checkerboard of 20-cell squares on vp and vs, four
+    vertical-force Ricker sources (f0 10 Hz, t0 0.12 s) evenly spaced at 20 m
+    depth, one receiver per column. Sources and receivers sit two cells deep:
+    the reference's derivative guards (solver/fdm.h:76-136) leave row 0
+    uncoupled, so a receiver at z = 0 records exact zeros."""
+    nx = nz = 200
+    h = 10.0
+    ii, jj = np.meshgrid(np.arange(nx), np.arange(nz), indexing="ij")
+    sign = np.where(((ii // 20) + (jj // 20)) % 2 == 0, 1.0, -1.0)
+    f = lambda a: np.ascontiguousarray(a.astype(np.float32).ravel())
+    vp, vs = f(3000.0 * (1 + 0.05 * sign)), f(1732.0 * (1 + 0.05 * sign))
+    rho = np.full(nx * nz, 2600.0, np.float32)
+    case = make_case(wave="psv", nx=nx, nz=nz, nt=nt, nsrc=nsrc, dx=h, dt=1e-3, f0=10.0, abs_width=20, sfe=10,
+                     model=(vp, vs, rho), angle=math.pi / 2, amp=1e10)
+    xmax = case["xmax"]
+    case["src"] = [[xmax * (s + 0.5) / nsrc, 2 * h, 0, 10.0, 0.12, math.pi / 2, 1e10] for s in range(nsrc)]
+    case["rec"] = [[i * h, 2 * h] for i in range(nx)]
+    case["nrec"] = nx
+    return case
+
+
 def lame(orc, case):
     """lambda, mu from vp, vs, rho with the oracle's vps2lm (float)."""
     lam, mu = orc.vps2lm(case["vp"], case["vs"], case["rho"])

@@ -21,26 +21,47 @@ def surface_receivers(case, h):
     return case
 
 
-def test_c1_full_psv_forward_matches_oracle(gpu, orc):
-    """P-SV 200x200 at 10 m, dt 1 ms, 2000 steps, receivers in every column,
-    through the cluster pass. FP32 round-off of the reference's scheme grows
-    over this run (the oracle's own FP32 and FP64 builds end ~1e-3 apart), so:
-    the first 1000 steps match the FP32 oracle to 1e-5, and over the whole
-    loop the GPU is as close to the FP64 solution as FP32 arithmetic in the
-    reference's order is (within a factor 2)."""
+@pytest.mark.parametrize("cluster", [1, 0])
+def test_c1_full_psv_forward_matches_oracle(gpu, orc, cluster):
+    """The 200x200 P-SV checkerboard (vp 3000, vs 1732, rho 2600, +-5 % in
+    20-cell squares), 4 shots, dt 1 ms, all 2000 steps, a receiver in every
+    column two cells deep, through the cluster pass and through the per-step
+    kernels: the displacement seismograms of every shot match the FP32 oracle
+    within relative L2 1e-5 over the whole time loop. On this model the
+    scheme is well conditioned: the oracle's own FP32 and FP64 builds stay
+    about 1.5e-6 apart over the 2000 steps."""
+    case = cases.checkerboard_case()
+    cfg, sol = cases.gpu_solver(gpu, case)
+    sol.set_option("cluster", cluster)
+    sol.run_forward_batch([0, 1, 2, 3])
+    assert (sol.stats().tile_tz < 0) == (cluster == 1), "unexpected kernel form"
+    pb = cases.oracle_problem(orc, case)
+    for s in range(4):
+        o32 = orc.forward(pb, s, adj=True)
+        for q, c in ((0, "x"), (2, "z")):
+            g = sol.out(c, slot=s)
+            assert np.abs(g).max() > 0, (s, c)
+            assert cases.rel(g, o32[q]) < 1e-5, (s, c)
+
+
+def test_jittered_layered_psv_short_run_matches_oracle(gpu, orc):
+    """P-SV 200x200 on a layered, faulted model with 3 % per-cell jitter,
+    800 steps. Over longer runs this model carries a mode of the reference
+    scheme that grows by about 0.75 % per step (shot 2's FP64 trace norm per
+    1000 steps: ~1e2 at steps 2000-3000, ~2e18 at steps 7000-8000), and the
+    oracle's FP32 and FP64 builds part from step ~1500 on (7.7e-4 over steps
+    1000-2000, 0.55 after), so no FP32 code holds a 1e-5 bar there. The
+    first 800 steps are well conditioned (FP32 to FP64: 7.9e-7)."""
     h = 10.0
-    case = surface_receivers(cases.make_case(wave="psv", nx=200, nz=200, nt=2000, nsrc=4, dx=h, dt=1e-3, f0=10.0,
+    case = surface_receivers(cases.make_case(wave="psv", nx=200, nz=200, nt=800, nsrc=4, dx=h, dt=1e-3, f0=10.0,
                                              abs_width=20, sfe=10, seed=1), h)
     cfg, sol = cases.gpu_solver(gpu, case)
     sol.run_forward_batch([0, 1, 2, 3])
     assert sol.stats().tile_tz < 0, "the cluster path did not run"
     pb = cases.oracle_problem(orc, case)
     o32 = orc.forward(pb, 2, adj=True)
-    o64 = orc.forward(pb, 2, adj=True, precision="f64")
     for q, c in ((0, "x"), (2, "z")):
-        g = sol.out(c, slot=2)
-        assert cases.rel(g[:, :1000], o32[q][:, :1000]) < 1e-5, c
-        assert cases.rel(g, o64[q]) <= 2.0 * cases.rel(o32[q], o64[q]), c
+        assert cases.rel(sol.out(c, slot=2), o32[q]) < 1e-5, c
 
 
 def test_c2_full_cluster_equals_step_kernels(gpu, orc):
