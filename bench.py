@@ -419,6 +419,9 @@ def run_ours(args, ws, rank, local):
         mp.close()
         sp.close()
 
+    hbm = None
+    if rank == 0 and not args.no_hbm_step:
+        hbm = [hbm_step(pkg, wave) for wave in ("psv", "sh")]
     ref_gpu = None
     if rank == 0 and ws == 1 and not args.no_ref_gpu:
         ref_gpu = _reference_gpu_leg(wl)
@@ -442,13 +445,51 @@ def run_ours(args, ws, rank, local):
                 "parallelism": "shots sharded over %d rank(s), replicas" % ws},
         "cell_updates_per_s": round(2.0 * cells * NT * NSHOT * args.steps * ws / (total_ms / 1e3), 1),
         "misfit": mis_val, "plain_path": plain, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
-        "reference_gpu": ref_gpu,
+        "reference_gpu": ref_gpu, "hbm_step": hbm,
         "breakdown_ms_per_gradient": {k: round(getattr(st, k) / args.steps, 3)
                                       for k in ("forward_ms", "adjoint_ms", "misfit_ms", "filter_ms")},
         "gpu_launches": int(st.launches), "clocks": clocks,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def hbm_step(pkg, wave, nx=4096, nz=1024, nshot=16, nt=40):
+    """The per-step marching kernel where the HBM roofline applies: a 16-shot
+    batch on the full-inversion grid (4096 x 1024 at 5 m, dt 0.4 ms, 256
+    receivers), forward, no checkpoints. The kernel configuration is tuned on
+    a first pass (the solver's autotuner), then three passes of `nt` steps are
+    timed with CUDA events in the solver's step windows (step kernels only).
+    achieved = algorithmic bytes per step (68 B P-SV / 40 B SH per cell and
+    shot: the state read and written once, the model read once) / time per
+    step. The state (16 x 12 or 7 fields of 16.8 MB) is far larger than L2."""
+    from tests import cases
+
+    case = cases.make_case(wave=wave, nx=nx, nz=nz, nt=nt, nsrc=nshot, nrec=256, dx=5.0, dt=4e-4, f0=12.0,
+                           abs_width=20, sfe=10, seed=5)
+    case["values"]["mode"] = 3
+    cfg, sol = cases.gpu_solver(pkg, case, extra={"cluster": 0})
+    sol.set_option("cluster", 0)
+    sol.set_option("batch", nshot)
+    shots = list(range(nshot))
+    sol.run_forward_batch(shots)  # tunes the configuration, warms up
+    sol.stats(reset=True)
+    for _ in range(3):
+        sol.run_forward_batch(shots)
+    st = sol.stats()
+    sol.close()
+    us = 1e3 * st.step_ms / max(st.step_launches, 1)
+    per_cell = 68.0 if wave == "psv" else 40.0
+    algo = per_cell * nx * nz * nshot
+    gbs = algo / (us * 1e-6) / 1e9
+    peak, kind = peaks()
+    return {"wave": wave, "grid": [nx, nz], "shots": nshot, "steps_timed": int(st.step_launches),
+            "kernel": "k_march (z-strip marching step, %d-row strips, %d-column chunks, bulk loads %d)" % (
+                st.tile_tz, st.tile_tx, st.march_bulk),
+            "us_per_step": round(us, 2), "algorithmic_bytes_per_step": algo, "achieved_gbs": round(gbs, 1),
+            "peak_gbs": peak, "frac": round(gbs / peak, 3), "peak_source": kind,
+            "cell_updates_per_s": round(nx * nz * nshot / (us * 1e-6), 1),
+            "traffic_bytes_per_step": profiled_traffic("march_%s_4096x1024x16" % wave)}
 
 
 # ----------------------------------------------------------------------------
@@ -810,6 +851,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-path leg")
     ap.add_argument("--no-ref-gpu", action="store_true", help="skip the reference-kernels-on-GPU leg")
+    ap.add_argument("--no-hbm-step", action="store_true", help="skip the per-step marching-kernel records")
     ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
                     help="c2 is the headline; the others print their own line")
     ap.add_argument("--shots", type=int, default=0, help="shot count for c3/c5 (default 64/16)")
