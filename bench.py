@@ -562,33 +562,24 @@ def run_c1(args):
 
 def run_c3(args):
     """P-SV 2048x1024, nt 6000: one gradient with FP32, BF16 and FP16
-    checkpoints; gradient differences against the FP32-checkpoint gradient."""
+    checkpoints; gradient differences against the FP32-checkpoint gradient.
+    Each precision's error against an FP64 oracle run on this grid and model
+    (one shot, 2000 steps) is a GPU test (tests/test_gpu_precision.py)."""
     import __graft_entry__ as ge
+    from tests import cases
 
     pkg = ge.load_package()
-    nx, nz, h, dt, nt = 2048, 1024, 5.0, 4e-4, 6000
     nshot = args.shots or 64
-    rng = np.random.default_rng(7)
-    def unit_field():
-        f = smooth(rng.standard_normal(nx * nz).astype(np.float32), nx, nz, 30.0)
-        return (f - f.min()) / (f.max() - f.min())
-
-    vp = (2000.0 + 2500.0 * unit_field()).astype(np.float32)
-    vs = (vp / (1.7 + 0.3 * unit_field())).astype(np.float32)
-    rho = (310.0 * vp ** 0.25).astype(np.float32)
-    xmax = (nx - 1) * h
-    src = [[xmax * (s + 0.5) / nshot, 4 * h, 0, 15.0, 0.08, math.pi / 2, 1e10] for s in range(nshot)]
-    rec = [[i * 4 * h, 2 * h] for i in range(nx // 4)]
-    values = {"mode": 2, "sh": 0, "psv": 1, "nt": nt, "dt": dt, "sfe": 50, "model_type": 0, "trace_type": 0,
-              "abs_left": 1, "abs_right": 1, "abs_bottom": 1, "abs_top": 0, "abs_width": 20, "abs_alpha": 0.015,
-              "inv_lambda": 1, "inv_mu": 1, "inv_rho": 1}
+    case = cases.random_smooth_case(nt=6000, nsrc=nshot)
+    nx, nz, h = case["nx"], case["nz"], 5.0
     tmp = tempfile.mkdtemp(prefix="gbfwi_c3_")
-    model = lame(vs, vp, rho)
+    values = dict(case["values"], mode=2)
+    model = lame(case["vs"], case["vp"], case["rho"])
     obs = None
     res = {}
     grads = {}
     for prec in (0, 1, 2):
-        cfg, sol = _solver_for(pkg, tmp, values, src, rec, nx, nz, h, model)
+        cfg, sol = _solver_for(pkg, tmp, values, case["src"], case["rec"], nx, nz, h, model)
         sol.set_option("ckpt", prec)
         if obs is None:
             obs = {"x": [], "z": []}
@@ -615,24 +606,26 @@ def run_c3(args):
         res[("fp32", "bf16", "fp16")[prec]]["grad_rel_diff_vs_fp32_ckpt"] = {
             n: float(np.linalg.norm(grads[prec][n] - grads[0][n]) / np.linalg.norm(grads[0][n]))
             for n in ("k_lambda", "k_mu", "k_rho")}
-    _line("shots/s fwd+adj by checkpoint precision (P-SV 2048x1024)", res["fp16"]["shots_per_s"], "shots/s",
+    _line("shots/s fwd+adj by checkpoint precision (P-SV 2048x1024)", res["bf16"]["shots_per_s"], "shots/s",
           {"workload": "P-SV 2048x1024 at 5 m, dt 0.4 ms, 6000 steps, %d shots f0 15 Hz, checkpoints every 50 "
                        "steps; smooth random vp 2000-4500, vp/vs 1.7-2.0" % nshot},
-          precision=res, note="FP64-oracle errors of each precision are measured on reduced grids in "
-                              "tests/test_gpu_precision.py")
+          precision=res, note="16-bit checkpoints hold the displacement differences the kernel accumulation "
+                              "reads; each precision's error against an FP64 oracle run on this grid and "
+                              "model is tests/test_gpu_precision.py::test_precision_study_grid_vs_fp64_oracle")
 
 
 def run_c4(args):
-    """Serving: forward+adjoint requests with Poisson arrivals, mixed P-SV/SH,
-    grid sides U[128,1024], 1000-5000 steps; p50/p99 latency and requests/s,
-    against the same requests solved one at a time."""
+    """Serving: forward+adjoint requests, mixed P-SV/SH, grid sides
+    U[128,1024], 1000-5000 steps. Three runs of the same seeded requests:
+    all queued at once (the engine's capacity: requests/s and
+    cell-updates/s), Poisson arrivals at --load x that capacity (p50/p99
+    latency), and the first --sequential of them solved one at a time (the
+    plain comparator)."""
     import __graft_entry__ as ge
 
     pkg = ge.load_package()
     nreq = args.requests
     rng = np.random.default_rng(11)
-    rate = args.rate
-    arrivals = np.cumsum(rng.exponential(1.0 / rate, nreq))
     # eight seeded layered, faulted models of 1024 x 1024; a request takes the
     # top-left nx x nz window of one of them
     bases = [[a.reshape(1024, 1024) for a in lame(*faulted_model(nx=1024, nz=1024, h=10.0, seed=100 + b,
@@ -648,34 +641,48 @@ def run_c4(args):
         rec = np.array([[i * 40.0, 20.0] for i in range(nx // 4)], np.float32)
         reqs.append(dict(psv=psv, nx=nx, nz=nz, dx=10.0, dt=8e-4, nt=nt, lam=lam, mu=mu, rho=rho, src=src,
                          rec=rec))
-    srv = pkg.Server(sfe=10, ckpt=2)
-    if args.server_tile:
-        srv.set_option("tile", args.server_tile)
-    for q, r in enumerate(reqs):
-        srv.submit(arrival=float(arrivals[q]), **r)
-    srv.run()
-    st = srv.stats()
-    # the same requests, one at a time (first `seq` of them)
+    cells = [2 * r["nx"] * r["nz"] * r["nt"] for r in reqs]
+
+    def serve(arrivals, max_slots=0, tile=0):
+        srv = pkg.Server(sfe=10, ckpt=2, max_slots=max_slots)
+        if tile:
+            srv.set_option("tile", tile)
+        for q, r in enumerate(reqs[:len(arrivals)]):
+            srv.submit(arrival=float(arrivals[q]), **r)
+        srv.run()
+        st = srv.stats()
+        srv.close()
+        return st
+
+    # capacity: every request queued at t = 0
+    sat = serve(np.zeros(nreq), tile=args.server_tile)
+    cap = sat.completed / sat.wall_s
+    # latency under load: Poisson arrivals at a fraction of that capacity
+    rate = args.rate if args.rate > 0 else args.load * cap
+    arrivals = np.cumsum(np.random.default_rng(12).exponential(1.0 / rate, nreq))
+    live = serve(arrivals, tile=args.server_tile)
+    # the plain comparator: the first `seq` requests one at a time, with the
+    # 2-D tile kernel (configuration 3, the faster choice for a lone grid of
+    # these sizes; the marching strips pay off with many requests in flight)
     seq = min(nreq, args.sequential)
-    one = pkg.Server(sfe=10, ckpt=2, max_slots=1)
-    # one request at a time: the 2-D tile kernel (configuration 3) is the
-    # faster choice for a lone grid of these sizes, the marching strips only
-    # pay off with many requests in flight
-    one.set_option("tile", 3)
-    for r in reqs[:seq]:
-        one.submit(arrival=0.0, **r)
-    one.run()
-    s1 = one.stats()
-    cells_seq = sum(2 * r["nx"] * r["nz"] * r["nt"] for r in reqs[:seq])
-    _line("served forward+adjoint requests/s", round(st.completed / st.wall_s, 3), "requests/s",
-          {"workload": "%d requests, Poisson arrivals at %.1f/s, 50/50 P-SV/SH, sides U[128,1024] at 10 m, "
-                       "1000-5000 steps (dt 0.8 ms), layered faulted models, FP16 checkpoints" % (nreq, rate)},
-          p50_latency_s=round(st.p50_s, 3), p99_latency_s=round(st.p99_s, 3), max_concurrent=st.max_concurrent,
-          wall_s=round(st.wall_s, 2), cell_updates_per_s=round(st.cell_updates / st.wall_s, 1),
-          sequential={"requests": seq, "wall_s": round(s1.wall_s, 2),
-                      "requests_per_s": round(seq / s1.wall_s, 3),
-                      "cell_updates_per_s": round(cells_seq / s1.wall_s, 1)},
-          gpu_launches=int(st.launches))
+    one = serve(np.zeros(seq), max_slots=1, tile=3)
+    cu_sat = sat.cell_updates / sat.wall_s
+    cu_seq = sum(cells[:seq]) / one.wall_s
+    _line("served forward+adjoint requests/s", round(cap, 3), "requests/s",
+          {"workload": "%d requests, 50/50 P-SV/SH, sides U[128,1024] at 10 m, 1000-5000 steps (dt 0.8 ms), "
+                       "layered faulted models, FP16 checkpoints" % nreq},
+          capacity={"requests_per_s": round(cap, 3), "cell_updates_per_s": round(cu_sat, 1),
+                    "wall_s": round(sat.wall_s, 2), "max_concurrent": sat.max_concurrent,
+                    "over_sequential_cell_updates": round(cu_sat / cu_seq, 2),
+                    "launches": int(sat.launches), "rounds": int(sat.rounds)},
+          under_load={"arrival_rate_per_s": round(rate, 3), "fraction_of_capacity": round(rate / cap, 3),
+                      "requests_per_s": round(live.completed / live.wall_s, 3),
+                      "p50_latency_s": round(live.p50_s, 3), "p99_latency_s": round(live.p99_s, 3),
+                      "max_concurrent": live.max_concurrent, "wall_s": round(live.wall_s, 2)},
+          sequential={"requests": seq, "wall_s": round(one.wall_s, 2), "requests_per_s": round(seq / one.wall_s, 3),
+                      "cell_updates_per_s": round(cu_seq, 1),
+                      "p50_latency_s_one_at_a_time": round(one.p50_s, 3)},
+          gpu_launches=int(sat.launches))
 
 
 def run_c5(args):
@@ -856,7 +863,9 @@ def main():
                     help="c2 is the headline; the others print their own line")
     ap.add_argument("--shots", type=int, default=0, help="shot count for c3/c5 (default 64/16)")
     ap.add_argument("--requests", type=int, default=512, help="c4 request count")
-    ap.add_argument("--rate", type=float, default=20.0, help="c4 Poisson arrival rate (requests/s)")
+    ap.add_argument("--rate", type=float, default=0.0,
+                    help="c4 Poisson arrival rate (requests/s); 0: --load x the measured capacity")
+    ap.add_argument("--load", type=float, default=0.8, help="c4 arrival rate as a fraction of capacity")
     ap.add_argument("--sequential", type=int, default=64, help="c4 requests also solved one at a time")
     ap.add_argument("--server-tile", type=int, default=0,
                     help="c4 step kernel configuration (0: the engine's default)")

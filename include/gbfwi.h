@@ -167,7 +167,11 @@ int gb_solver_batch_capacity(gb_solver *s);
  * adjoint round, default; 0: forward, misfit and adjoint one after another),
  * "cluster_qm" (columns per
  * thread of the cluster pass: 0 = chosen with the cluster size, or 4, 8, 10,
- * 12, 16, 20, 24), "hbm_budget_gb". Options
+ * 12, 16, 20, 24), "snap_async" (1: wavefield snapshots are copied on the
+ * device into a ring of staging buffers and written to their files by a
+ * writer thread while the time loop goes on, default; 0: a blocking copy and
+ * write per field, as the reference does; either way every file is written
+ * when the call returns), "hbm_budget_gb". Options
  * change no forward result; "ckpt" changes kernels by the checkpoint
  * rounding and "cluster" by the order in which shots are summed. */
 int gb_solver_set_option(gb_solver *s, const char *key, double value);

@@ -23,7 +23,7 @@ LIB = os.path.join(HERE, "libgbfwi.so")
 EXE = os.path.join(HERE, "gbinv")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-LIB_SOURCES = ["gb_step.cu", "gb_march.cu", "gb_cluster.cu", "gb_aux.cu", "gb_misfit.cu", "gb_solver.cu", "gb_server.cu", "gb_abi.cu", "gb_config.cpp",
+LIB_SOURCES = ["gb_step.cu", "gb_march.cu", "gb_cluster.cu", "gb_aux.cu", "gb_misfit.cu", "gb_solver.cu", "gb_snapshot.cu", "gb_server.cu", "gb_abi.cu", "gb_config.cpp",
                "gb_optimizer.cpp"]
 EXE_SOURCES = ["gbinv.cpp"]
 

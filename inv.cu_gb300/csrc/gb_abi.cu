@@ -344,6 +344,8 @@ int gb_solver_set_option(gb_solver *s, const char *key, double value) {
         v.opt_snap = value != 0;
     } else if (k == "pipeline") {
         v.opt_pipe = value != 0;
+    } else if (k == "snap_async") {
+        v.opt_snap_async = value != 0;
     } else if (k == "tma") {
         v.opt_tma = value != 0;
         v.invalidate_graphs();

@@ -117,6 +117,26 @@ inline float ckpt_scale_of(float amax, int prec) {
     return ldexpf(1.f, e - 1);
 }
 
+// Fields of one checkpoint of a wave system. FP32 keeps the reference's
+// fields (solver/fdm.h:521-560): SH uy, vy; P-SV ux, uz, vx, vz. The 16-bit
+// forms keep what the kernel accumulation reads of the forward wavefield
+// instead (solver/fdm.h:583-606), computed in FP32 from the displacement
+// before rounding: SH d(uy)/dx, d(uy)/dz, vy; P-SV the divergence
+// d(ux)/dx + d(uz)/dz, the normal-strain difference d(ux)/dx - d(uz)/dz, the
+// shear sum d(ux)/dz + d(uz)/dx, vx, vz. A difference of two 16-bit
+// displacements loses the digits the two values share, and so does a sum of
+// two rounded normal strains where they cancel (shear waves); each rounded
+// strain here keeps its own relative precision. An SH+P-SV slot stores the
+// SH fields first.
+#ifdef __CUDACC__
+__host__ __device__
+#endif
+inline int ckpt_nf_sh(int prec) { return prec == 0 ? 2 : 3; }
+#ifdef __CUDACC__
+__host__ __device__
+#endif
+inline int ckpt_nf_psv(int prec) { return prec == 0 ? 4 : 5; }
+
 // Packed tile CSR header: [0]=ntiles [1]=nentries [2]=ntraces, then
 // tile_ptr[ntiles+1], local[nentries], tptr[nentries+1], traces[ntraces].
 inline int csr_words(int ntiles, int nent, int ntr) { return 3 + ntiles + 1 + nent + nent + 1 + ntr; }

@@ -513,7 +513,7 @@ long long gb_server_submit(gb_server *h, const gb_request_desc *d) {
     r.id = (long long)S.reqs.size();
     r.d = *d;
     r.ncomp = d->psv ? 2 : 1;
-    r.nf = d->psv ? 4 : 2;
+    r.nf = d->psv ? ckpt_nf_psv(S.prec) : ckpt_nf_sh(S.prec);
     r.nsfe = d->nt / S.sfe;
     r.bytes = S.footprint(*d, r.nf, r.nsfe, r.ncomp);
     if ((double)r.bytes > S.budget) {

@@ -181,6 +181,7 @@ int Solver::init(const Config &cfg, int nx_, int nz_, float xmax_, float zmax_) 
     if (cfg.has("cluster_shift")) opt_shift = cfg.iv("cluster_shift") != 0;
     if (cfg.has("cluster_snap")) opt_snap = cfg.iv("cluster_snap") != 0;
     if (cfg.has("pipeline")) opt_pipe = cfg.iv("pipeline") != 0;
+    if (cfg.has("snap_async")) opt_snap_async = cfg.iv("snap_async") != 0;
     if (cfg.has("cluster")) opt_cluster = std::max(0, std::min(16, cfg.iv("cluster")));
     nx = nx_;
     nz = nz_;
@@ -294,6 +295,7 @@ int Solver::init(const Config &cfg, int nx_, int nz_, float xmax_, float zmax_) 
 
 void Solver::release() {
     if (st) cudaStreamSynchronize(st);
+    snapw.close();
     invalidate_graphs();
     for (auto &b : slots) {
         cudaFree(b.state);
@@ -419,7 +421,7 @@ size_t Solver::slot_bytes(int prec) const {
     size_t b = ((sh ? NSH : 0) + (psv ? NPSV : 0)) * n * 4;
     const int ncomp = (sh ? 1 : 0) + (psv ? 2 : 0);
     b += (size_t)ncomp * nrec * nt * 4 * (adj ? 2 : 1);
-    if (adj && nsfe) b += (size_t)nsfe * nf() * n * (prec == CKPT_F32 ? 4 : 2) + (size_t)nsfe * nf() * 4;
+    if (adj && nsfe) b += (size_t)nsfe * nf(prec) * n * (prec == CKPT_F32 ? 4 : 2) + (size_t)nsfe * nf(prec) * 4;
     return b;
 }
 
@@ -561,9 +563,9 @@ int Solver::ensure_slots(int n) {
             if (b.ckpt_prec == opt_ckpt) continue;
             cudaFree(b.ckpt);
             cudaFree(b.amax);
-            const size_t elems = (size_t)nsfe * nf() * nc;
+            const size_t elems = (size_t)nsfe * nf(opt_ckpt) * nc;
             GB_CUDA_TRY(cudaMalloc(&b.ckpt, elems * (opt_ckpt == CKPT_F32 ? 4 : 2)));
-            GB_CUDA_TRY(cudaMalloc(&b.amax, (size_t)nsfe * nf() * 4));
+            GB_CUDA_TRY(cudaMalloc(&b.amax, (size_t)nsfe * nf(opt_ckpt) * 4));
             b.ckpt_prec = opt_ckpt;
             invalidate_graphs();
         }
@@ -655,8 +657,8 @@ int Solver::fill_slots(int kind, const int *shots, int n, bool record_u) {
         S.sfe = sfe;
         S.ckpt_write = kind == PASS_FWD;
         S.nsfe = nsfe;
-        S.nf = nf();
         S.ckpt_prec = B.ckpt_prec < 0 ? CKPT_F32 : B.ckpt_prec;
+        S.nf = nf(S.ckpt_prec);
         if (kind == PASS_ADJ) {
             S.inj = d_csr + rec_inj_set;
             S.inj_x = B.adstf[0];
@@ -709,7 +711,7 @@ int Solver::enqueue_pass(int kind, int n, bool snapshot, int snap_isrc) {
     const bool ck = kind == PASS_FWD && adj && nsfe > 0;
     const bool q16 = ck && opt_ckpt != CKPT_F32;
     if (q16)
-        for (int b = 0; b < n; b++) GB_CUDA_TRY(cudaMemsetAsync(slots[b].amax, 0, (size_t)nsfe * nf() * 4, st));
+        for (int b = 0; b < n; b++) GB_CUDA_TRY(cudaMemsetAsync(slots[b].amax, 0, (size_t)nsfe * nf(opt_ckpt) * 4, st));
     // timing window: consecutive steps with no other kernel between them
     int w0 = 0, w1 = std::min(nt, 64);
     if (ck) w1 = std::min(w1, sfe - 1);
@@ -855,6 +857,14 @@ int Solver::run_pass(int kind, int n, bool snapshot, int snap_isrc) {
     }
     GB_CUDA_TRY(cudaEventRecord(ev_pass1, st));
     GB_CUDA_TRY(cudaStreamSynchronize(st));
+    if (snapshot && opt_snap_async) {
+        std::string msg;
+        const int rc = snapw.drain(&msg);
+        if (rc) {
+            set_error("snapshot export: " + msg);
+            return rc;
+        }
+    }
     if (tile.threads) stats.march_bulk = use_tma() ? 1 : 0;
     if (use_tma() && tile.threads && march_tma_error()) {
         set_error("marching kernel: a bulk-load wait ran out of iterations; the pass is invalid");
@@ -1232,6 +1242,15 @@ int Solver::export_data(const std::string &comp, const float *d_data, int n) {
     return write_bin(path + "/output/proc" + pad6(n) + "_" + comp + ".bin", h.data(), ncell());
 }
 
+// One snapshot field: through the asynchronous writer (gb_snapshot.h), or a
+// blocking copy and write (opt_snap_async = 0).
+int Solver::export_field(const std::string &comp, const float *d_data, int n) {
+    if (!opt_snap_async) return export_data(comp, d_data, n);
+    GB_CUDA_TRY(snapw.open(ncell()));
+    GB_CUDA_TRY(snapw.push(st, d_data, path + "/output/proc" + pad6(n) + "_" + comp + ".bin"));
+    return GB_OK;
+}
+
 // FdmSolver::exportSnapshot (solver/fdm.h:312-347), slot 0.
 int Solver::export_snapshot(int it, int isrc, int par) {
     std::string istr;
@@ -1249,13 +1268,13 @@ int Solver::export_snapshot(int it, int isrc, int par) {
     float *psp = sh ? p + (size_t)NSH * nc : p;
     int rc = GB_OK;
     if (trace_type == 0) {
-        if (sh && !rc) rc = export_data("vy" + istr, shp + (size_t)(VY0 + par) * nc, it + 1);
-        if (psv && !rc) rc = export_data("vx" + istr, psp + (size_t)(VX0 + par) * nc, it + 1);
-        if (psv && !rc) rc = export_data("vz" + istr, psp + (size_t)(VZ0 + par) * nc, it + 1);
+        if (sh && !rc) rc = export_field("vy" + istr, shp + (size_t)(VY0 + par) * nc, it + 1);
+        if (psv && !rc) rc = export_field("vx" + istr, psp + (size_t)(VX0 + par) * nc, it + 1);
+        if (psv && !rc) rc = export_field("vz" + istr, psp + (size_t)(VZ0 + par) * nc, it + 1);
     } else if (trace_type == 1) {
-        if (sh && !rc) rc = export_data("uy" + istr, shp + (size_t)UY * nc, it + 1);
-        if (psv && !rc) rc = export_data("ux" + istr, psp + (size_t)UX * nc, it + 1);
-        if (psv && !rc) rc = export_data("uz" + istr, psp + (size_t)UZ * nc, it + 1);
+        if (sh && !rc) rc = export_field("uy" + istr, shp + (size_t)UY * nc, it + 1);
+        if (psv && !rc) rc = export_field("ux" + istr, psp + (size_t)UX * nc, it + 1);
+        if (psv && !rc) rc = export_field("uz" + istr, psp + (size_t)UZ * nc, it + 1);
     }
     return rc;
 }

@@ -11,6 +11,7 @@
 
 #include "gb_config.h"
 #include "gb_internal.h"
+#include "gb_snapshot.h"
 #include "gbfwi.h"
 
 namespace gb {
@@ -73,6 +74,8 @@ struct Solver {
     int opt_shift = 1;    // cluster passes: row-shifted shared-memory layout (no bank conflicts) when it fits
     int opt_snap = 1;     // cluster adjoint: store the adjoint state, accumulate the kernels after the pass
     int opt_cluster = 1;  // cluster-resident passes: 0 never, 1 automatic R, 2..16 this cluster size
+    int opt_snap_async = 1;  // snapshots through the asynchronous writer (0: blocking copy per field)
+    SnapWriter snapw;
 
     // device buffers in the reference layout
     float *lambda = nullptr, *mu = nullptr, *rho = nullptr;
@@ -133,7 +136,8 @@ struct Solver {
     int init_kernels();
     // --- helpers
     size_t ncell() const { return (size_t)nx * nz; }
-    int nf() const { return (sh ? 2 : 0) + (psv ? 4 : 0); }
+    // checkpoint fields per snapshot at precision prec (ckpt_nf_sh/psv)
+    int nf(int prec) const { return (sh ? ckpt_nf_sh(prec) : 0) + (psv ? ckpt_nf_psv(prec) : 0); }
     size_t slot_bytes(int prec) const;
     int fill_slots(int kind, const int *shots, int n, bool record_u);
     int enqueue_pass(int kind, int n, bool snapshot, int snap_isrc);
@@ -164,6 +168,7 @@ struct Solver {
     int book_forward_pass();
     int export_snapshot(int it, int isrc, int par);
     int export_data(const std::string &comp, const float *d_data, int n);
+    int export_field(const std::string &comp, const float *d_data, int n);
     void invalidate_graphs();
     cudaError_t record_timing(cudaEvent_t e);
     int max_tiles() const { return ((nz + tile.tz - 1) / tile.tz) * ((nx + tile.tx - 1) / tile.tx); }

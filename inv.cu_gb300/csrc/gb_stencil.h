@@ -60,6 +60,20 @@ __device__ __forceinline__ float st_kmu_psv(float k, float dvxdx, float dvxdz, f
     const float shear = __fmul_rn(dvxdz + dvzdx, fzdx + fxdz);
     return fmaf(-fmaf(2.f * dvxdx, fxdx, fmaf(2.f * dvzdz, fzdz, shear)), ndt, k);
 }
+// The P-SV kernels from the forward strains of a 16-bit checkpoint: the
+// divergence dv = dxux_fw + dzuz_fw, the difference dd = dxux_fw - dzuz_fw
+// and the shear sum sh = dxuz_fw + dzux_fw. 2 a x + 2 b z with x = (dv + dd)/2,
+// z = (dv - dd)/2 is (a + b) dv + (a - b) dd, so
+//   k_mu     -= ((dxux + dzuz) dv + (dxux - dzuz) dd + (dzux + dxuz) sh) ndt
+//   k_lambda -= (dxux + dzuz) dv ndt
+__device__ __forceinline__ float st_kmu_psv_strain(float k, float dvxdx, float dvxdz, float dvzdx, float dvzdz,
+                                                   float fdv, float fdd, float fsh, float ndt) {
+    const float c = fmaf(dvxdx + dvzdz, fdv, fmaf(dvxdx - dvzdz, fdd, __fmul_rn(dvxdz + dvzdx, fsh)));
+    return fmaf(-c, ndt, k);
+}
+__device__ __forceinline__ float st_klambda_psv_strain(float k, float dvxdx, float dvzdz, float fdv, float ndt) {
+    return fmaf(-__fmul_rn(dvxdx + dvzdz, fdv), ndt, k);
+}
 // P-SV: k_lambda -= (dxux + dzuz)(dxux_fw + dzuz_fw) ndt
 __device__ __forceinline__ float st_klambda_psv(float k, float dvxdx, float dvzdz, float fxdx, float fzdz, float ndt) {
     return fmaf(-__fmul_rn(dvxdx + dvzdz, fxdx + fzdz), ndt, k);

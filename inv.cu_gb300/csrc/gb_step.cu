@@ -373,33 +373,72 @@ cudaError_t launch_step(bool psv, TileCfg tc, const Slot *d_slots, int nslots, i
 // Forward checkpoints (solver/fdm.h:521-533,552-560): at the step with
 // (it+1) % sfe == 0, displacement is saved before the step and velocity after
 // it, into slot isfe = nsfe - (it+1)/sfe. Storage is FP32, BF16 or FP16; the
-// 16-bit forms use one power-of-two scale per snapshot and field, derived
-// from the field's max |value|, so the scaling itself adds no rounding.
+// 16-bit forms store the displacement's differences that the kernel
+// accumulation reads instead of the displacement (ckpt_nf_sh/psv), and use
+// one power-of-two scale per snapshot and field, derived from the field's
+// max |value|, so the scaling itself adds no rounding.
 __device__ __forceinline__ float ckpt_scale(float amax, int prec) { return ckpt_scale_of(amax, prec); }
 
-// Fields of one checkpoint group: q index in the slot's checkpoint and the
-// state array that feeds it.
-__device__ __forceinline__ int ckpt_fields(const Slot &S, bool psv, int which_u, int par, const float **src,
-                                           int *q) {
-    const bool has_sh = S.sh[0] != nullptr;
+// The fields of one checkpoint group (displacement before the step,
+// which_u = 1, or velocity after it, which_u = 0) of one wave system: their
+// index in the slot's checkpoint and how each is formed from the state.
+struct CkGroup {
+    int nfld;
+    int q[3];
+    int kind;  // 0: copies of a, b; 1: SH d/dx, d/dz of a; 2: P-SV strains of a = ux, b = uz
+    const float *a, *b;
+};
+
+__device__ __forceinline__ CkGroup ckpt_group(const Slot &S, bool psv, int which_u, int par) {
+    CkGroup g;
+    const bool q16 = S.ckpt_prec != CKPT_F32;
     if (!psv) {
-        src[0] = which_u ? S.sh[UY] : S.sh[VY0 + par];
-        q[0] = which_u ? 0 : 1;
-        return 1;
+        g.kind = (which_u && q16) ? 1 : 0;
+        g.a = which_u ? S.sh[UY] : S.sh[VY0 + par];
+        g.b = nullptr;
+        if (q16) {
+            g.nfld = which_u ? 2 : 1;
+            g.q[0] = which_u ? 0 : 2;
+            g.q[1] = 1;
+        } else {
+            g.nfld = 1;
+            g.q[0] = which_u ? 0 : 1;
+        }
+        return g;
     }
-    const int base = has_sh ? 2 : 0;
-    if (which_u) {
-        src[0] = S.psv[UX];
-        src[1] = S.psv[UZ];
-        q[0] = base + 0;
-        q[1] = base + 1;
+    const int base = S.sh[0] != nullptr ? ckpt_nf_sh(S.ckpt_prec) : 0;
+    g.a = which_u ? S.psv[UX] : S.psv[VX0 + par];
+    g.b = which_u ? S.psv[UZ] : S.psv[VZ0 + par];
+    g.kind = (which_u && q16) ? 2 : 0;
+    if (q16) {
+        g.nfld = which_u ? 3 : 2;
+        for (int f = 0; f < g.nfld; f++) g.q[f] = base + (which_u ? 0 : 3) + f;
     } else {
-        src[0] = S.psv[VX0 + par];
-        src[1] = S.psv[VZ0 + par];
-        q[0] = base + 2;
-        q[1] = base + 3;
+        g.nfld = 2;
+        for (int f = 0; f < 2; f++) g.q[f] = base + (which_u ? 0 : 2) + f;
     }
-    return 2;
+    return g;
+}
+
+// Field f of group g at cell k, in FP32: a copy, or the forward-staggered
+// differences of the kernel accumulation (the guards and arithmetic of
+// k_interaction's FP32 path: 0 where the reference skips a difference).
+__device__ __forceinline__ float ckpt_value(const Slot &S, const CkGroup &g, int f, size_t k) {
+    if (g.kind == 0) return __ldg((f == 0 ? g.a : g.b) + k);
+    const int nx = S.nx, nz = S.nz;
+    const int i = (int)(k / nz), j = (int)(k - (size_t)i * nz);
+    const bool gx = i >= 1 && i < nx - 2, gz = j >= 1 && j < nz - 2;
+    auto ddx = [&](const float *w) {
+        return gx ? dplus(__ldg(w + k + nz), __ldg(w + k), __ldg(w + k + 2 * nz), __ldg(w + k - nz), S.c9x, S.c24x)
+                  : 0.f;
+    };
+    auto ddz = [&](const float *w) {
+        return gz ? dplus(__ldg(w + k + 1), __ldg(w + k), __ldg(w + k + 2), __ldg(w + k - 1), S.c9z, S.c24z) : 0.f;
+    };
+    if (g.kind == 1) return f == 0 ? ddx(g.a) : ddz(g.a);
+    if (f == 2) return ddx(g.b) + ddz(g.a);  // d(uz)/dx + d(ux)/dz, summed as st_kmu_psv sums them
+    const float exx = ddx(g.a), ezz = ddz(g.b);
+    return f == 0 ? exx + ezz : exx - ezz;  // divergence, normal-strain difference
 }
 
 // Checkpoint slot of step index k for slot S, or -1 when k is not a
@@ -420,26 +459,24 @@ __global__ void k_ckpt_amax(const Slot *__restrict__ slots, int kstep, int which
     const int isfe = ckpt_slot(S, kstep, &par);
     if (isfe < 0) return;
     if (psv ? S.psv[0] == nullptr : S.sh[0] == nullptr) return;
-    const float *src[2];
-    int q[2];
-    const int nfld = ckpt_fields(S, psv, which_u, par, src, q);
+    const CkGroup g = ckpt_group(S, psv, which_u, par);
     const size_t n = (size_t)S.nx * S.nz;
-    __shared__ float red[2][32];
-    for (int f = 0; f < nfld; f++) {
+    __shared__ float red[3][32];
+    for (int f = 0; f < g.nfld; f++) {
         float m = 0.f;
         for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
-            m = fmaxf(m, fabsf(__ldg(src[f] + k)));
+            m = fmaxf(m, fabsf(ckpt_value(S, g, f, k)));
         for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
         if ((threadIdx.x & 31) == 0) red[f][threadIdx.x >> 5] = m;
     }
     __syncthreads();
     if (threadIdx.x < 32) {
-        for (int f = 0; f < nfld; f++) {
+        for (int f = 0; f < g.nfld; f++) {
             float m = threadIdx.x < (blockDim.x >> 5) ? red[f][threadIdx.x] : 0.f;
             for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
             // non-negative floats order like their bit patterns
             if (threadIdx.x == 0)
-                atomicMax(reinterpret_cast<unsigned *>(S.ckpt_amax) + (size_t)isfe * S.nf + q[f], __float_as_uint(m));
+                atomicMax(reinterpret_cast<unsigned *>(S.ckpt_amax) + (size_t)isfe * S.nf + g.q[f], __float_as_uint(m));
         }
     }
 }
@@ -450,26 +487,24 @@ __global__ void k_ckpt_store(const Slot *__restrict__ slots, int kstep, int whic
     const int isfe = ckpt_slot(S, kstep, &par);
     if (isfe < 0) return;
     if (psv ? S.psv[0] == nullptr : S.sh[0] == nullptr) return;
-    const float *src[2];
-    int q[2];
-    const int nfld = ckpt_fields(S, psv, which_u, par, src, q);
+    const CkGroup g = ckpt_group(S, psv, which_u, par);
     const size_t n = (size_t)S.nx * S.nz;
-    for (int f = 0; f < nfld; f++) {
-        const size_t off = ((size_t)isfe * S.nf + q[f]) * n;
+    for (int f = 0; f < g.nfld; f++) {
+        const size_t off = ((size_t)isfe * S.nf + g.q[f]) * n;
         if (S.ckpt_prec == CKPT_F32) {
             float *dst = static_cast<float *>(S.ckpt) + off;
             for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
-                dst[k] = __ldg(src[f] + k);
+                dst[k] = ckpt_value(S, g, f, k);
         } else {
-            const float sc = ckpt_scale(S.ckpt_amax[(size_t)isfe * S.nf + q[f]], S.ckpt_prec);
+            const float sc = ckpt_scale(S.ckpt_amax[(size_t)isfe * S.nf + g.q[f]], S.ckpt_prec);
             if (S.ckpt_prec == CKPT_BF16) {
                 __nv_bfloat16 *dst = static_cast<__nv_bfloat16 *>(S.ckpt) + off;
                 for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
-                    dst[k] = __float2bfloat16_rn(__ldg(src[f] + k) * sc);
+                    dst[k] = __float2bfloat16_rn(ckpt_value(S, g, f, k) * sc);
             } else {
                 __half *dst = static_cast<__half *>(S.ckpt) + off;
                 for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
-                    dst[k] = __float2half_rn(__ldg(src[f] + k) * sc);
+                    dst[k] = __float2half_rn(ckpt_value(S, g, f, k) * sc);
             }
         }
     }
@@ -530,10 +565,11 @@ __global__ void k_interaction(const Slot *__restrict__ slots, const KernelGroup 
         const int par = (S.par0 + kstep + 1) & 1;  // velocity written by this step
         const float ndt = (float)S.sfe * S.dt;
         const float c9x = S.c9x, c24x = S.c24x, c9z = S.c9z, c24z = S.c24z;
-        const int base = (PSV && S.sh[0] != nullptr) ? 2 : 0;
-        const int nfu = PSV ? 2 : 1;
-        float inv[4];
-        for (int q = 0; q < 2 * nfu; q++) {
+        const bool q16 = S.ckpt_prec != CKPT_F32;
+        const int base = (PSV && S.sh[0] != nullptr) ? ckpt_nf_sh(S.ckpt_prec) : 0;
+        const int nfs = PSV ? ckpt_nf_psv(S.ckpt_prec) : ckpt_nf_sh(S.ckpt_prec);
+        float inv[5];
+        for (int q = 0; q < nfs; q++) {
             const float a = S.ckpt_amax ? S.ckpt_amax[(size_t)isfe * S.nf + base + q] : 0.f;
             inv[q] = 1.f / ckpt_scale(a, S.ckpt_prec);
         }
@@ -552,25 +588,44 @@ __global__ void k_interaction(const Slot *__restrict__ slots, const KernelGroup 
                              c9z, c24z)
                      : 0.f;
         };
+        auto ck = [&](int q) { return ck_load(S, isfe, base + q, k, n, inv[q]); };
         if (PSV) {
-            float dvxdx, dvxdz, dvzdx, dvzdz, fxdx, fxdz, fzdx, fzdz;
+            float dvxdx, dvxdz, dvzdx, dvzdz;
             grad(S.psv[UX], dvxdx, dvxdz);
             grad(S.psv[UZ], dvzdx, dvzdz);
-            grad_ck(0, fxdx, fxdz);
-            grad_ck(1, fzdx, fzdz);
+            // forward: FP32 displacement (differences taken here), or the
+            // stored strains: divergence, normal-strain difference, shear sum (16-bit)
+            float fxdx = 0.f, fxdz = 0.f, fzdx = 0.f, fzdz = 0.f, fdv = 0.f, fdd = 0.f, fsh = 0.f;
+            if (q16) {
+                fdv = ck(0);
+                fdd = ck(1);
+                fsh = ck(2);
+            } else {
+                grad_ck(0, fxdx, fxdz);
+                grad_ck(1, fzdx, fzdz);
+            }
             if (G.inv_rho) {
-                const float vx_fw = ck_load(S, isfe, base + 2, k, n, inv[2]);
-                const float vz_fw = ck_load(S, isfe, base + 3, k, n, inv[3]);
+                const float vx_fw = ck(q16 ? 3 : 2);
+                const float vz_fw = ck(q16 ? 4 : 3);
                 kr = st_krho_psv(kr, vx_fw, __ldg(S.psv[VX0 + par] + k), vz_fw, __ldg(S.psv[VZ0 + par] + k), ndt);
             }
-            if (G.inv_mu) km = st_kmu_psv(km, dvxdx, dvxdz, dvzdx, dvzdz, fxdx, fxdz, fzdx, fzdz, ndt);
-            if (G.inv_lambda) kl = st_klambda_psv(kl, dvxdx, dvzdz, fxdx, fzdz, ndt);
+            if (G.inv_mu)
+                km = q16 ? st_kmu_psv_strain(km, dvxdx, dvxdz, dvzdx, dvzdz, fdv, fdd, fsh, ndt)
+                         : st_kmu_psv(km, dvxdx, dvxdz, dvzdx, dvzdz, fxdx, fxdz, fzdx, fzdz, ndt);
+            if (G.inv_lambda)
+                kl = q16 ? st_klambda_psv_strain(kl, dvxdx, dvzdz, fdv, ndt)
+                         : st_klambda_psv(kl, dvxdx, dvzdz, fxdx, fzdz, ndt);
         } else {
             float dvydx, dvydz, fdx, fdz;
             grad(S.sh[UY], dvydx, dvydz);
-            grad_ck(0, fdx, fdz);
+            if (q16) {
+                fdx = ck(0);
+                fdz = ck(1);
+            } else {
+                grad_ck(0, fdx, fdz);
+            }
             if (G.inv_rho) {
-                const float vy_fw = ck_load(S, isfe, 1, k, n, inv[1]);
+                const float vy_fw = ck(q16 ? 2 : 1);
                 kr = st_krho_sh(kr, vy_fw, __ldg(S.sh[VY0 + par] + k), ndt);
             }
             if (G.inv_mu) km = st_kmu_sh(km, dvydx, fdx, dvydz, fdz, ndt);

@@ -77,6 +77,59 @@ def checkerboard_case(nt=2000, nsrc=4):
     return case
 
 
+def smooth_field(nx, nz, cells, rng):
+    """A seeded random field smoothed by a separable Gaussian of `cells`
+    cells, scaled to [0, 1] (float32, reference layout)."""
+    a = rng.standard_normal((nx, nz))
+    r = int(3 * cells)
+    w = np.exp(-0.5 * (np.arange(-r, r + 1) / cells) ** 2)
+    w /= w.sum()
+    pad = np.pad(a, r, mode="wrap")
+    t = sum(w[q] * pad[q:q + nx, :] for q in range(2 * r + 1))
+    t = sum(w[q] * t[:, q:q + nz] for q in range(2 * r + 1))
+    t = (t - t.min()) / (t.max() - t.min())
+    return np.ascontiguousarray(t.astype(np.float32).ravel())
+
+
+def random_smooth_case(nx=2048, nz=1024, nt=6000, nsrc=64, seed=7, cells=30.0):
+    """The P-SV precision-study configuration: 5 m cells, dt 0.4 ms,
+    checkpoints every 50 steps, a smooth random model with vp 2000-4500 m/s
+    and vp/vs 1.7-2.0 (Gardner density), f0 15 Hz vertical-force sources at
+    20 m depth, a receiver every 4th column at 10 m depth."""
+    rng = np.random.default_rng(seed)
+    vp = (2000.0 + 2500.0 * smooth_field(nx, nz, cells, rng)).astype(np.float32)
+    vs = (vp / (1.7 + 0.3 * smooth_field(nx, nz, cells, rng))).astype(np.float32)
+    rho = (310.0 * vp ** 0.25).astype(np.float32)
+    h = 5.0
+    case = make_case(wave="psv", nx=nx, nz=nz, nt=nt, nsrc=nsrc, dx=h, dt=4e-4, f0=15.0, abs_width=20, sfe=50,
+                     model=(vp, vs, rho), angle=math.pi / 2, amp=1e10)
+    xmax = case["xmax"]
+    case["src"] = [[xmax * (s + 0.5) / nsrc, 4 * h, 0, 15.0, 0.08, math.pi / 2, 1e10] for s in range(nsrc)]
+    case["rec"] = [[i * 4 * h, 2 * h] for i in range(nx // 4)]
+    case["nrec"] = len(case["rec"])
+    return case
+
+
+def fp64_gradient(orc, pb, obs, tw, wave):
+    """Kernels of the waveform misfit from the oracle's FP64 forward and
+    adjoint, the adjoint source 2 r tw (r = (syn - obs) tw, time-reversed,
+    misfit/waveform.h:4-40) formed in double."""
+    comps = "xz" if wave == "psv" else "y"
+    kern = None
+    for s in range(pb.nsrc):
+        ox, oy, oz, ck = orc.forward(pb, s, adj=True, precision="f64")
+        syn = {"x": ox, "y": oy, "z": oz}
+        ad = {}
+        for c in "xyz":
+            if c in comps:
+                r = (syn[c] - obs[c][s].astype(np.float64)) * tw
+                ad[c] = np.ascontiguousarray((2 * r * tw)[:, ::-1])
+            else:
+                ad[c] = np.zeros((pb.nrec, pb.nt))
+        kern = orc.adjoint(pb, [ad["x"], ad["y"], ad["z"]], ck, kern, precision="f64")
+    return kern
+
+
 def lame(orc, case):
     """lambda, mu from vp, vs, rho with the oracle's vps2lm (float)."""
     lam, mu = orc.vps2lm(case["vp"], case["vs"], case["rho"])

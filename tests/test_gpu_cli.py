@@ -131,3 +131,24 @@ def test_mode1_writes_snapshots_and_supershot_traces(gpu, orc, tmp_path):
         assert snap.size == 201 * 201 and np.isfinite(snap).all() and np.abs(snap).max() > 0
     tr, _ = orc.read_su(os.path.join(out, "vy_000000.su"))
     assert tr.shape == (132, 400)
+
+
+@pytest.mark.parametrize("mode,key", [(1, "wfe"), (2, "wae")])
+def test_async_snapshots_equal_blocking_ones(gpu, orc, tmp_path, mode, key):
+    """Wavefield snapshots through the asynchronous writer (default) and
+    through a blocking copy per field (snap_async = 0) give the same files,
+    byte for byte, and all of them exist when the command returns: mode 1
+    (forward, every wfe steps) and mode 2 (adjoint, every wae steps)."""
+    files = {}
+    for snap_async in (1, 0):
+        d = str(tmp_path / ("m%d_a%d" % (mode, snap_async)))
+        write_checker(d, orc, nsrc=2, extra={"nt": 400.0, key: 50.0})
+        gbinv(gpu, d, "-mode=%d" % mode, "-snap_async=%d" % snap_async)
+        out = os.path.join(d, "output")
+        names = sorted(f for f in os.listdir(out) if f.startswith("proc") and f.endswith(".bin")
+                       and f.split("_", 1)[1][:2] in ("vx", "vy", "vz", "ux", "uy", "uz"))
+        files[snap_async] = {f: open(os.path.join(out, f), "rb").read() for f in names}
+    assert len(files[1]) >= 8, sorted(files[1])
+    assert files[1].keys() == files[0].keys()
+    for f in files[1]:
+        assert files[1][f] == files[0][f], f
