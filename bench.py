@@ -686,38 +686,108 @@ def run_c4(args):
 
 
 def run_c5(args):
-    """P-SV 4096x1024, nt 8000, 4096 receivers: one gradient of a reduced shot
-    set with FP16 checkpoints (the full 128-shot, 20-iteration inversion does
-    not fit a benchmark run)."""
+    """P-SV 4096x1024 at 5 m, dt 0.4 ms, 8000 steps, 4096 receivers, on the
+    faulted model of the headline workload generated at this grid. Without
+    --iterations: one gradient of --shots shots (default 16) with FP16
+    checkpoints. With --iterations N: the full inversion's setting (--shots,
+    default 128; L-BFGS with memory 10; smoothing sigma 10 cells; lambda and
+    mu inverted; initial model the true one smoothed by a Gaussian of 500 m)
+    for N iterations, once with BF16 checkpoints and once with FP32 ones,
+    reporting the time per iteration, the misfit history and the difference
+    between the two final models."""
     import __graft_entry__ as ge
 
     pkg = ge.load_package()
     nx, nz, h, dt, nt = 4096, 1024, 5.0, 4e-4, 8000
-    nshot = args.shots or 16
+    inversion = args.iterations > 0
+    nshot = args.shots or (128 if inversion else 16)
     vs, vp, rho = faulted_model(nx=nx, nz=nz, h=h, seed=SEED, vs_bottom=3500.0)
     xmax = (nx - 1) * h
     src = [[xmax * (s + 0.5) / nshot, 4 * h, 0, 12.0, 0.1, math.pi / 2, 1e10] for s in range(nshot)]
     rec = [[i * h, 2 * h] for i in range(nx)]
     values = {"mode": 2, "sh": 0, "psv": 1, "nt": nt, "dt": dt, "sfe": 50, "model_type": 0, "trace_type": 0,
               "abs_left": 1, "abs_right": 1, "abs_bottom": 1, "abs_top": 0, "abs_width": 20, "abs_alpha": 0.015,
-              "inv_lambda": 1, "inv_mu": 1, "inv_rho": 1}
+              "inv_lambda": 1, "inv_mu": 1, "inv_rho": 1 if not inversion else 0, "misfit": 0, "filter": 0,
+              "filter_sigma": 10, "optimizer": 1, "lbfgs_mem": 10, "lbfgs_thresh": 0.0,
+              "inv_iteration": max(args.iterations, 1), "inv_cycle": 0, "ls_step": 10, "ls_step_max": 0.5,
+              "ls_step_init": 0.05, "ls_thresh": 1.2}
     tmp = tempfile.mkdtemp(prefix="gbfwi_c5_")
-    cfg, sol = _solver_for(pkg, tmp, values, src, rec, nx, nz, h, lame(vs, vp, rho))
-    sol.set_option("ckpt", 2)
-    obs = {"x": np.zeros((nshot, nx, nt), np.float32), "z": np.zeros((nshot, nx, nt), np.float32)}
-    mis = pkg.Misfit.from_obs(0, sol, obs, pkg.GaussianFilter(nx, nz, 10))
-    sol.timer_begin()
-    mis.run(kernel=True)
-    ms = sol.timer_end()
-    st = sol.stats()
-    per_launch = st.step_ms / max(st.step_launches, 1)
-    cells = nx * nz * min(nshot, st.batch_capacity)
-    _line("shots/s fwd+adj (P-SV 4096x1024 gradient)", round(nshot / (ms / 1e3), 3), "shots/s",
-          {"workload": "P-SV 4096x1024 at 5 m, dt 0.4 ms, 8000 steps, %d shots, 4096 receivers, FP16 "
-                       "checkpoints every 50 steps, smoothing sigma 10" % nshot},
-          ms_per_step=round(ms, 1), batch=st.batch_capacity, tile=[st.tile_tz, st.tile_tx],
-          step_kernel={"avg_launch_us": round(per_launch * 1e3, 2),
-                       "achieved_gbs": round(68.0 * cells / (per_launch * 1e-3) / 1e9, 1)})
+    os.makedirs(os.path.join(tmp, "output"), exist_ok=True)
+    true = lame(vs, vp, rho)
+    desc = ("P-SV 4096x1024 at 5 m, dt 0.4 ms, 8000 steps, %d shots f0 12 Hz, 4096 receivers, checkpoints every "
+            "50 steps, smoothing sigma 10" % nshot)
+    if not inversion:
+        cfg, sol = _solver_for(pkg, tmp, values, src, rec, nx, nz, h, true)
+        sol.set_option("ckpt", 2)
+        obs = {"x": np.zeros((nshot, nx, nt), np.float32), "z": np.zeros((nshot, nx, nt), np.float32)}
+        mis = pkg.Misfit.from_obs(0, sol, obs, pkg.GaussianFilter(nx, nz, 10))
+        sol.timer_begin()
+        mis.run(kernel=True)
+        ms = sol.timer_end()
+        st = sol.stats()
+        per_launch = st.step_ms / max(st.step_launches, 1)
+        cells = nx * nz * min(nshot, st.batch_capacity)
+        _line("shots/s fwd+adj (P-SV 4096x1024 gradient)", round(nshot / (ms / 1e3), 3), "shots/s",
+              {"workload": desc + ", FP16 checkpoints"},
+              ms_per_step=round(ms, 1), batch=st.batch_capacity, tile=[st.tile_tz, st.tile_tx],
+              step_kernel={"avg_launch_us": round(per_launch * 1e3, 2),
+                           "achieved_gbs": round(68.0 * cells / (per_launch * 1e-3) / 1e9, 1)})
+        return
+    from scipy.ndimage import gaussian_filter
+
+    init_v = [np.ascontiguousarray(gaussian_filter(a.reshape(nx, nz).astype(np.float64), 500.0 / h,
+                                                   mode="nearest").astype(np.float32).ravel())
+              for a in (vs, vp, rho)]
+    init = lame(*init_v)
+    # observed data on the true model (setup)
+    cfg, sol = _solver_for(pkg, tmp, values, src, rec, nx, nz, h, true)
+    obs = {"x": np.empty((nshot, nx, nt), np.float32), "z": np.empty((nshot, nx, nt), np.float32)}
+    cap = sol.capacity
+    for a0 in range(0, nshot, cap):
+        shots = list(range(a0, min(nshot, a0 + cap)))
+        sol.run_forward_batch(shots)
+        for q, s_ in enumerate(shots):
+            obs["x"][s_] = sol.out("x", slot=q)
+            obs["z"][s_] = sol.out("z", slot=q)
+    sol.close()
+    res = {}
+    models = {}
+    for prec, name in ((1, "bf16"), (0, "fp32")):
+        cfg, sol = _solver_for(pkg, tmp, values, src, rec, nx, nz, h, init)
+        sol.set_option("ckpt", prec)
+        mis = pkg.Misfit.from_obs(0, sol, obs, pkg.GaussianFilter(nx, nz, 10))
+        opt = pkg.Optimizer(cfg, sol, mis)
+        t0 = time.perf_counter()
+        opt.run()
+        wall = time.perf_counter() - t0
+        hist = opt.history()
+        ev = opt.evaluations()
+        models[name] = sol.model()
+        st = sol.stats()
+        res[name] = {"wall_s": round(wall, 1), "s_per_iteration": round(wall / args.iterations, 1),
+                     "misfit_history": [float("%.6g" % v) for v in hist],
+                     "evaluations": len(ev), "batch": st.batch_capacity}
+        opt.close()
+        mis.close()
+        sol.close()
+
+    def rel(a, b):
+        return float(np.linalg.norm(a.astype(np.float64) - b) / np.linalg.norm(b.astype(np.float64)))
+
+    for name in ("bf16", "fp32"):
+        res[name]["model_error_vs_true"] = {k: rel(models[name][k], true[q]) for q, k in enumerate(("lambda", "mu"))}
+    res["bf16_vs_fp32_model"] = {k: rel(models["bf16"][k], models["fp32"][k]) for k in ("lambda", "mu")}
+    res["bf16_vs_fp32_update"] = {
+        k: float(np.linalg.norm(models["bf16"][k].astype(np.float64) - models["fp32"][k]) /
+                 np.linalg.norm(models["fp32"][k].astype(np.float64) - init[q]))
+        for q, k in enumerate(("lambda", "mu"))}
+    res["initial_model_error_vs_true"] = {k: rel(init[q], true[q]) for q, k in enumerate(("lambda", "mu"))}
+    _line("full inversion, s per L-BFGS iteration (P-SV 4096x1024, %d shots)" % nshot,
+          res["bf16"]["s_per_iteration"], "s/iteration",
+          {"workload": desc + ", L-BFGS memory 10, %d of 20 iterations, BF16 vs FP32 checkpoints, initial "
+                       "model smoothed by a 500 m Gaussian" % args.iterations},
+          higher_is_better=False, inversion=res,
+          projected_20_iterations_s=round(20 * res["bf16"]["s_per_iteration"], 0))
 
 
 def run_profile_case(args):
@@ -861,7 +931,9 @@ def main():
     ap.add_argument("--no-hbm-step", action="store_true", help="skip the per-step marching-kernel records")
     ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
                     help="c2 is the headline; the others print their own line")
-    ap.add_argument("--shots", type=int, default=0, help="shot count for c3/c5 (default 64/16)")
+    ap.add_argument("--shots", type=int, default=0,
+                    help="shot count for c3/c5 (default 64; c5 16, or 128 with --iterations)")
+    ap.add_argument("--iterations", type=int, default=0, help="c5: run that many L-BFGS iterations of the inversion")
     ap.add_argument("--requests", type=int, default=512, help="c4 request count")
     ap.add_argument("--rate", type=float, default=0.0,
                     help="c4 Poisson arrival rate (requests/s); 0: --load x the measured capacity")

@@ -253,6 +253,7 @@ int gb_misfit_set_obs(gb_misfit *m, const float *obs_x, const float *obs_y, cons
 int gb_misfit_run(gb_misfit *m, int kernel, int snapshot, double *value);
 /* Per-trace misfit values of the last run, [nsrc][nrec][ncomp]. */
 int gb_misfit_trace_values(gb_misfit *m, double *out, size_t n);
+/* Frees the misfit; it may come before or after gb_solver_destroy of its solver. */
 void gb_misfit_destroy(gb_misfit *m);
 
 /* --------------------------------------------------------------- Optimizer
@@ -286,6 +287,7 @@ int gb_optimizer_evaluations(gb_optimizer *o, double *out, int n);
 double gb_linesearch_step(int optimizer, const double *lens, const double *vals, int ls_count, const double *gtg,
                           const double *gtp, int inv_count, int step_count, int ls_step, double ls_thresh,
                           double step_max, int *status);
+/* Frees the optimizer; it may come before or after gb_solver_destroy of its solver. */
 void gb_optimizer_destroy(gb_optimizer *o);
 
 /* ----------------------------------------------------------------- Serving

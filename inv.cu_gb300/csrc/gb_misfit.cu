@@ -635,7 +635,8 @@ int gb_misfit_trace_values(gb_misfit *m, double *out, size_t n) {
 
 void gb_misfit_destroy(gb_misfit *m) {
     if (!m) return;
-    if (m->s && m->s->st) cudaStreamSynchronize(m->s->st);
+    // the solver may already be destroyed: wait for the device instead of its stream
+    cudaDeviceSynchronize();
     for (int c = 0; c < 3; c++) cudaFree(m->obs[c]);
     cudaFree(m->tw);
     cudaFree(m->d_tr);

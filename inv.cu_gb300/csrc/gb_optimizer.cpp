@@ -637,7 +637,8 @@ int gb_optimizer_evaluations(gb_optimizer *o, double *out, int n) {
 
 void gb_optimizer_destroy(gb_optimizer *o) {
     if (!o) return;
-    if (o->s && o->s->st) cudaStreamSynchronize(o->s->st);
+    // the solver may already be destroyed: wait for the device instead of its stream
+    cudaDeviceSynchronize();
     for (int ip = 0; ip < 3; ip++)
         for (float *v : {o->m_old[ip], o->g_old[ip], o->p_new[ip], o->p_old[ip]}) cudaFree(v);
     for (float *p : o->owned) cudaFree(p);

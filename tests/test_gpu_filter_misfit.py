@@ -180,3 +180,19 @@ def test_lbfgs_without_memory_is_rejected(gpu, tmp_path):
         gpu.Optimizer(cfg, sol, mis)
     mis.close()
     sol.close()
+
+
+def test_misfit_and_optimizer_may_outlive_their_solver(gpu, orc):
+    """Destroying a solver before the misfit and the optimizer built on it
+    is allowed: their destruction does not touch the solver."""
+    case = cases.make_case(wave="sh", nx=64, nz=48, nt=100, nsrc=2, nrec=16, sfe=10, seed=3)
+    case["values"].update({"optimizer": 1, "inv_iteration": 1, "lbfgs_mem": 2, "ls_step": 2, "ls_step_max": 0.5,
+                           "ls_step_init": 0.05, "ls_thresh": 1.2})
+    cfg, sol = cases.gpu_solver(gpu, case)
+    obs = {"y": np.zeros((2, 16, 100), np.float32)}
+    m = gpu.Misfit.from_obs(0, sol, obs)
+    opt = gpu.Optimizer(cfg, sol, m)
+    m.run(kernel=True)
+    sol.close()
+    opt.close()
+    m.close()
