@@ -658,30 +658,35 @@ def run_c4(args):
     sat = serve(np.zeros(nreq), tile=args.server_tile)
     cap = sat.completed / sat.wall_s
     # latency under load: Poisson arrivals at a fraction of that capacity
+    # (--load 0 skips this run)
     rate = args.rate if args.rate > 0 else args.load * cap
-    arrivals = np.cumsum(np.random.default_rng(12).exponential(1.0 / rate, nreq))
-    live = serve(arrivals, tile=args.server_tile)
+    live = None
+    if rate > 0:
+        arrivals = np.cumsum(np.random.default_rng(12).exponential(1.0 / rate, nreq))
+        live = serve(arrivals, tile=args.server_tile)
     # the plain comparator: the first `seq` requests one at a time, with the
     # 2-D tile kernel (configuration 3, the faster choice for a lone grid of
     # these sizes; the marching strips pay off with many requests in flight)
+    # (--sequential 0 skips it)
     seq = min(nreq, args.sequential)
-    one = serve(np.zeros(seq), max_slots=1, tile=3)
+    one = serve(np.zeros(seq), max_slots=1, tile=3) if seq > 0 else None
     cu_sat = sat.cell_updates / sat.wall_s
-    cu_seq = sum(cells[:seq]) / one.wall_s
+    cu_seq = sum(cells[:seq]) / one.wall_s if one else None
     _line("served forward+adjoint requests/s", round(cap, 3), "requests/s",
           {"workload": "%d requests, 50/50 P-SV/SH, sides U[128,1024] at 10 m, 1000-5000 steps (dt 0.8 ms), "
                        "layered faulted models, FP16 checkpoints" % nreq},
           capacity={"requests_per_s": round(cap, 3), "cell_updates_per_s": round(cu_sat, 1),
                     "wall_s": round(sat.wall_s, 2), "max_concurrent": sat.max_concurrent,
-                    "over_sequential_cell_updates": round(cu_sat / cu_seq, 2),
+                    "over_sequential_cell_updates": round(cu_sat / cu_seq, 2) if cu_seq else None,
                     "launches": int(sat.launches), "rounds": int(sat.rounds)},
-          under_load={"arrival_rate_per_s": round(rate, 3), "fraction_of_capacity": round(rate / cap, 3),
-                      "requests_per_s": round(live.completed / live.wall_s, 3),
-                      "p50_latency_s": round(live.p50_s, 3), "p99_latency_s": round(live.p99_s, 3),
-                      "max_concurrent": live.max_concurrent, "wall_s": round(live.wall_s, 2)},
-          sequential={"requests": seq, "wall_s": round(one.wall_s, 2), "requests_per_s": round(seq / one.wall_s, 3),
-                      "cell_updates_per_s": round(cu_seq, 1),
-                      "p50_latency_s_one_at_a_time": round(one.p50_s, 3)},
+          under_load=None if live is None else {
+              "arrival_rate_per_s": round(rate, 3), "fraction_of_capacity": round(rate / cap, 3),
+              "requests_per_s": round(live.completed / live.wall_s, 3),
+              "p50_latency_s": round(live.p50_s, 3), "p99_latency_s": round(live.p99_s, 3),
+              "max_concurrent": live.max_concurrent, "wall_s": round(live.wall_s, 2)},
+          sequential=None if one is None else {
+              "requests": seq, "wall_s": round(one.wall_s, 2), "requests_per_s": round(seq / one.wall_s, 3),
+              "cell_updates_per_s": round(cu_seq, 1), "p50_latency_s_one_at_a_time": round(one.p50_s, 3)},
           gpu_launches=int(sat.launches))
 
 
