@@ -56,6 +56,11 @@ constexpr int kStageCols = 4, kStages = kRing / kStageCols;
 // traces; a tile with more walks the lists in global memory.
 constexpr int kInjStage = 256, kCsrStage = 256;
 constexpr int kCsrStageWords = 5 * kCsrStage + 2;
+// The x-absorbing factor of the chunk's velocity columns (c0-1 .. c1+1) is
+// staged in shared memory before the march (chunks of at most kAxStage - 3
+// columns), so the per-column velocity update reads it there instead of
+// waiting on a global load.
+constexpr int kAxStage = 264;
 static_assert(kStageCols == TMAP_BOX_COLS, "bulk-load box width");
 
 // 4-byte async copy to shared address `d` (a 32-bit shared-window address);
@@ -106,19 +111,19 @@ __device__ __forceinline__ void tma_col(unsigned dst, const void *tmap, int z0, 
 }
 
 // Words staged per column step: stress at p (NS), velocity, displacement and
-// reciprocal density at p-1 (2 NV + 1), the x-absorbing factor at p-1,
-// moduli at p-3.
+// reciprocal density at p-1 (2 NV + 1), moduli at p-3 (the x-absorbing
+// factor comes from the chunk's staged copy).
 template <bool PSV>
 struct MarchWords {
     static constexpr int NS = PSV ? 3 : 2, NV = PSV ? 2 : 1;
-    static constexpr int SG = 0, V = NS, U = NS + NV, RHO = NS + 2 * NV, AX = RHO + 1, MU = AX + 1,
-                         LAM = MU + 1, N = PSV ? LAM + 1 : MU + 1;
+    static constexpr int SG = 0, V = NS, U = NS + NV, RHO = NS + 2 * NV, MU = RHO + 1, LAM = MU + 1,
+                         N = PSV ? LAM + 1 : MU + 1;
 };
 
 template <bool PSV>
 __host__ __device__ constexpr int march_smem_words(int threads) {
     return (kRing * MarchWords<PSV>::N + 2 * ((PSV ? 2 : 1) + (PSV ? 2 : 1))) * threads + 2 * 2 * (2 + 2) * 2 +
-           (PSV ? 2 : 1) * kInjStage + kCsrStageWords;
+           (PSV ? 2 : 1) * kInjStage + kCsrStageWords + kAxStage;
 }
 
 // TMA = false: each thread stages its own row with 4-byte cp.async.
@@ -143,6 +148,8 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
     float *s_vz = s_sz + 2 * NZS * TP;                   // [2][NV][TP]
     // [NV][kInjStage] behind s_vz (its address is recomputed where it is read)
     auto inj_stage = [&]() { return smem + kRing * W::N * blockDim.x + 2 * (NZS + NV) * (blockDim.x + 4); };
+    // [kAxStage] behind the staged lists: ax of columns c0-1 .. c1+1
+    auto ax_stage = [&]() { return inj_stage() + NV * kInjStage + kCsrStageWords; };
 
     // Blocks run shot-minor (block b: shot b % nslots, tile b / nslots): the
     // same strip of every shot runs close together, so the model columns,
@@ -256,6 +263,10 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
             for (int k = t; k <= nr; k += T) sr_tp[k] = rec_tptr[rec_ptr + k] - r0;
             for (int e = t; e < tr; e += T) sr_tr[e] = rec_traces[r0 + e];
         }
+        {
+            float *s_axc = ax_stage();
+            for (int k = t; k < c1 - c0 + 3; k += T) s_axc[k] = __ldg(S.ax + min(max(c0 - 1 + k, 0), nx - 1));
+        }
         if (t == 0) {
             s_inj_meta[0] = stage_i ? 0 : i0;  // trace index of s_inj[0]
             s_inj_meta[1] = stage_i ? ti : 0;  // staged values
@@ -299,7 +310,6 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
             cpa4(rs + (W::U + f) * T * 4, u[f] + kv, uo);
         }
         cpa4(rs + W::RHO * T * 4, rinv_g + kv, cv);
-        cpa4(rs + W::AX * T * 4, ax + (cv ? pv : 0), cv);
         const int pm = p - 3;
         const bool cm = pm >= c0 && pm < c1 && rowown;
         const int km = cm ? pm * nz + jj : 0;
@@ -403,7 +413,7 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
     // P-SV: unrolled by the queue depth, so the register queues rotate by
     // renaming (fewer registers and moves); SH keeps the rolled loop, which
     // fits its registers better
-    constexpr int kUnroll = (PSV || TMA) ? 4 : 1;
+    constexpr int kUnroll = PSV ? 4 : 1;
 #pragma unroll kUnroll
     for (int q = 0; q < nstep; q++) {
         const int p = p_first + q;
@@ -506,7 +516,7 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
                 inj_next = inj_ptr < inj_end ? inj_local[inj_ptr] : 0x7fffffff;
             }
             if ((unsigned)pv < (unsigned)nx && rowin) {
-                const float ab = (TMA ? __ldg(ax + pv) : cur[W::AX]) * azj;
+                const float ab = ax_stage()[pv - (c0 - 1)] * azj;
                 const float rinv = cur[W::RHO];
 #pragma unroll
                 for (int f = 0; f < NV; f++) vn[f] = st_velocity(ab, dt, ds[f], rinv, cur[W::V + f]);
@@ -624,7 +634,8 @@ static cudaError_t launch_march_t(dim3 grid, int threads, size_t smem, const Slo
 cudaError_t launch_march(bool psv, bool tma, int threads, int chunk, const Slot *d_slots, int nslots, int max_tiles,
                          int k, cudaStream_t st) {
     if (nslots <= 0 || max_tiles <= 0) return cudaSuccess;
-    if (threads < 32 || threads > kMaxMarchThreads || threads % 32 || chunk < 1) return cudaErrorInvalidValue;
+    if (threads < 32 || threads > kMaxMarchThreads || threads % 32 || chunk < 1 || chunk + 3 > kAxStage)
+        return cudaErrorInvalidValue;
     const dim3 grid(max_tiles, nslots);
     const size_t smem = (size_t)(psv ? march_smem_words<true>(threads) : march_smem_words<false>(threads)) * 4;
     if (psv)
