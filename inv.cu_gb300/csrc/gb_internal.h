@@ -27,6 +27,12 @@ enum CkptPrec { CKPT_F32 = 0, CKPT_BF16 = 1, CKPT_F16 = 2 };
 // memory. A batch is an array of slots; blockIdx.y selects the slot.
 struct Slot {
     int nx, nz, nt;
+    // address pitch of the slot's state and model arrays: cell (i, j) lies at
+    // i*pz + j; pz == nz is the reference layout (the solver), a larger pz
+    // (rows nz .. pz-1 unused) lets a served request of any nz use tensor maps
+    // (column starts on 16-byte boundaries). Checkpoints, traces and kernels
+    // keep the reference layout.
+    int pz;
     int tiles_z, tiles_x;
     int active;
     // Time base: a launch with step index k advances this slot from step

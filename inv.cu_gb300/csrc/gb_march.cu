@@ -160,7 +160,7 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
     const int it = S.it_base + kstep;
     if (it < 0 || it >= S.nt) return;
     const int par = (S.par0 + kstep) & 1;
-    const int nx = S.nx, nz = S.nz, nt = S.nt;
+    const int nx = S.nx, nz = S.nz, nt = S.nt, pz = S.pz;  // pz: address pitch of the grid arrays
     const int tile = (int)(blk / gridDim.y);
     if (tile >= S.tiles_z * S.tiles_x) return;
     const int strip = tile % S.tiles_z, ck = tile / S.tiles_z;
@@ -297,12 +297,12 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
     auto issue = [&](int p, int slot) {
         const unsigned rs = ring_row + (unsigned)(slot * W::N * T) * 4u;
         const bool cs = (unsigned)p < (unsigned)nx && rowin;
-        const int ks = cs ? p * nz + jj : 0;
+        const int ks = cs ? p * pz + jj : 0;
 #pragma unroll
         for (int f = 0; f < NS; f++) cpa4(rs + (W::SG + f) * T * 4, sig_in[f] + ks, cs);
         const int pv = p - 1;
         const bool cv = (unsigned)pv < (unsigned)nx && rowin && pv >= c0 - 1;
-        const int kv = cv ? pv * nz + jj : 0;
+        const int kv = cv ? pv * pz + jj : 0;
         const bool uo = cv && rowown && pv >= c0 && pv < c1;
 #pragma unroll
         for (int f = 0; f < NV; f++) {
@@ -312,7 +312,7 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
         cpa4(rs + W::RHO * T * 4, rinv_g + kv, cv);
         const int pm = p - 3;
         const bool cm = pm >= c0 && pm < c1 && rowown;
-        const int km = cm ? pm * nz + jj : 0;
+        const int km = cm ? pm * pz + jj : 0;
         cpa4(rs + W::MU * T * 4, mu + km, cm);
         if (PSV) cpa4(rs + W::LAM * T * 4, lam + km, cm);
     };
@@ -527,7 +527,7 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
 #pragma unroll
                 for (int f = 0; f < NV; f++) un[f] = st_displacement(cur[W::U + f], vn[f], dt);
                 if (rowown) {
-                    const int kv = pv * nz + j;
+                    const int kv = pv * pz + j;
 #pragma unroll
                     for (int f = 0; f < NV; f++) {
                         v_out[f][kv] = vn[f];
@@ -575,7 +575,7 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
         const int pm = p - 3;
         if (pm >= c0 && pm < c1 && rowown) {
             const bool xV = pm >= 1 && pm < nx - 2;
-            const int km = pm * nz + j;
+            const int km = pm * pz + j;
             const float m = cur[W::MU];
             if (PSV) {
                 const float dvxdx = xV ? dplus_m(vq[2][0], vq[1][0], vq[3][0], vq[0][0], c9x, c24x) : 0.f;

@@ -62,6 +62,8 @@ struct Req {
     TraceRefS *refs = nullptr;
     int *csr_src = nullptr, *csr_rin = nullptr, *csr_rec = nullptr;
     int nsfe = 0, nf = 0, ncomp = 0;
+    int pz = 0;              // address pitch of the state and model arrays
+    void *tmaps = nullptr;   // tensor maps of the fields (bulk loads), or null
     // progress
     int phase = 0;  // 0 waiting, 1 forward, 2 adjoint, 3 done
     int it = 0;
@@ -77,6 +79,10 @@ size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 struct Server {
     int sfe = 10, prec = CKPT_F32, max_slots = 64;
     TileCfg tile = {0, 0, 0};  // step kernel configuration (set at creation)
+    // bulk tensor loads in the marching kernel: requested (option "tma"), and
+    // still possible (every admitted request's maps could be encoded)
+    bool opt_tma = true, tma_ok = true;
+    bool use_tma() const { return opt_tma && tma_ok && tile.threads > 0; }
     double budget = 0;
     size_t used = 0;
     cudaStream_t st = nullptr;
@@ -94,15 +100,18 @@ struct Server {
     long long rounds = 0, launches = 0;
     double run_s = 0;
 
+    // State and model arrays are allocated at a pitch of nz rounded up to a
+    // multiple of 4 (the most admit() uses).
     size_t footprint(const gb_request_desc &d, int nf, int nsfe, int ncomp) const {
-        const size_t n = (size_t)d.nx * d.nz;
+        const size_t n = (size_t)d.nx * d.nz, np = (size_t)d.nx * ((d.nz + 3) & ~3);
         const size_t tr = (size_t)d.nrec * d.nt;
         const int nfield = d.psv ? NPSV : NSH;
         size_t b = 0;
-        b += align256(4 * n * 4);                                  // lam mu rho rinv
+        b += align256(4 * np * 4);                                 // lam mu rho rinv
         b += align256((size_t)(d.nx + d.nz) * 4);                  // ax az
         b += align256((size_t)3 * d.nt * 4);                       // stf
-        b += align256((size_t)nfield * n * 4);                     // state
+        b += align256((size_t)nfield * np * 4);                    // state
+        b += align256((size_t)TMAP_N * TMAP_BYTES);                // tensor maps
         b += 3 * align256((size_t)ncomp * tr * 4);                 // out, adstf, obs
         b += align256(3 * n * 4);                                  // kernels
         b += align256((size_t)d.nt * 4);                           // taper
@@ -205,6 +214,10 @@ void ricker1(int nt, float dt, const float *cfg, float *sx, float *sy, float *sz
 int admit(Server &S, Req &r) {
     const gb_request_desc &d = r.d;
     const size_t n = (size_t)d.nx * d.nz, tr = (size_t)d.nrec * d.nt;
+    // the marching kernel reads columns that start on 16-byte boundaries: a
+    // pitch of nz rounded up to a multiple of 4 (the 2-D tile kernel uses nz)
+    r.pz = S.tile.threads > 0 ? (d.nz + 3) & ~3 : d.nz;
+    const size_t np = (size_t)d.nx * r.pz;
     GB_CUDA_TRY(cudaMallocAsync((void **)&r.blk, r.bytes, S.st));
     char *p = r.blk;
     auto take = [&](size_t b) {
@@ -212,15 +225,16 @@ int admit(Server &S, Req &r) {
         p += align256(b);
         return q;
     };
-    r.lam = (float *)take(4 * n * 4);
-    r.mu = r.lam + n;
-    r.rho = r.lam + 2 * n;
-    r.rinv = r.lam + 3 * n;
+    r.lam = (float *)take(4 * np * 4);
+    r.mu = r.lam + np;
+    r.rho = r.lam + 2 * np;
+    r.rinv = r.lam + 3 * np;
     r.ax = (float *)take((size_t)(d.nx + d.nz) * 4);
     r.az = r.ax + d.nx;
     r.stf = (float *)take((size_t)3 * d.nt * 4);
     const int nfield = d.psv ? NPSV : NSH;
-    r.state = (float *)take((size_t)nfield * n * 4);
+    r.state = (float *)take((size_t)nfield * np * 4);
+    void *maps = take((size_t)TMAP_N * TMAP_BYTES);
     const int comps_psv[2] = {0, 2}, comps_sh[1] = {1};
     const int *cs = d.psv ? comps_psv : comps_sh;
     float *outb = (float *)take((size_t)r.ncomp * tr * 4);
@@ -269,10 +283,29 @@ int admit(Server &S, Req &r) {
 
     // uploads (pageable sources are staged by the runtime; they stay valid
     // until the request completes, by the API contract)
-    GB_CUDA_TRY(cudaMemcpyAsync(r.lam, d.lambda, n * 4, cudaMemcpyHostToDevice, S.st));
-    GB_CUDA_TRY(cudaMemcpyAsync(r.mu, d.mu, n * 4, cudaMemcpyHostToDevice, S.st));
-    GB_CUDA_TRY(cudaMemcpyAsync(r.rho, d.rho, n * 4, cudaMemcpyHostToDevice, S.st));
-    GB_CUDA_TRY(launch_reciprocal(r.rinv, r.rho, n, S.st));
+    // model columns at the pitch; rows nz .. pz-1 are never read (the step
+    // kernels stop at row nz, the bulk loads' tensors end there)
+    if (r.pz != d.nz) GB_CUDA_TRY(cudaMemsetAsync(r.lam, 0, 4 * np * 4, S.st));
+    const float *src[3] = {d.lambda, d.mu, d.rho};
+    float *dst[3] = {r.lam, r.mu, r.rho};
+    for (int q = 0; q < 3; q++)
+        GB_CUDA_TRY(cudaMemcpy2DAsync(dst[q], (size_t)r.pz * 4, src[q], (size_t)d.nz * 4, (size_t)d.nz * 4, d.nx,
+                                      cudaMemcpyHostToDevice, S.st));
+    GB_CUDA_TRY(launch_reciprocal(r.rinv, r.rho, np, S.st));
+    // tensor maps of the state and model fields for the marching kernel's
+    // bulk loads, for its strips of S.tile.threads rows
+    r.tmaps = nullptr;
+    std::vector<char> hmaps((size_t)TMAP_N * TMAP_BYTES);
+    if (S.use_tma()) {
+        const float *sh_state = d.psv ? nullptr : r.state, *psv_state = d.psv ? r.state : nullptr;
+        if (encode_slot_maps(hmaps.data(), d.psv ? psv_state : sh_state, !d.psv, d.psv != 0, r.rinv, r.mu, r.lam,
+                             d.nx, d.nz, r.pz, S.tile.threads)) {
+            GB_CUDA_TRY(cudaMemcpyAsync(maps, hmaps.data(), hmaps.size(), cudaMemcpyHostToDevice, S.st));
+            r.tmaps = maps;
+        } else {
+            S.tma_ok = false;  // this request's fields cannot be described: per-row loads from now on
+        }
+    }
     GB_CUDA_TRY(cudaMemcpyAsync(r.ax, hax.data(), d.nx * 4, cudaMemcpyHostToDevice, S.st));
     GB_CUDA_TRY(cudaMemcpyAsync(r.az, haz.data(), d.nz * 4, cudaMemcpyHostToDevice, S.st));
     GB_CUDA_TRY(cudaMemcpyAsync(r.stf, hstf.data(), hstf.size() * 4, cudaMemcpyHostToDevice, S.st));
@@ -283,7 +316,7 @@ int admit(Server &S, Req &r) {
         GB_CUDA_TRY(cudaMemcpyAsync(obb, d.obs, (size_t)r.ncomp * tr * 4, cudaMemcpyHostToDevice, S.st));
     else
         GB_CUDA_TRY(cudaMemsetAsync(obb, 0, (size_t)r.ncomp * tr * 4, S.st));
-    GB_CUDA_TRY(cudaMemsetAsync(r.state, 0, (size_t)nfield * n * 4, S.st));
+    GB_CUDA_TRY(cudaMemsetAsync(r.state, 0, (size_t)nfield * np * 4, S.st));
     GB_CUDA_TRY(cudaMemsetAsync(kb, 0, 3 * n * 4, S.st));
     GB_CUDA_TRY(cudaMemsetAsync(r.amax, 0, (size_t)r.nsfe * r.nf * 4, S.st));
     GB_CUDA_TRY(cudaMemsetAsync(outb, 0, (size_t)r.ncomp * tr * 4, S.st));
@@ -308,6 +341,8 @@ void fill_slot(const Server &S, const Req &r, Slot &s) {
     const gb_request_desc &d = r.d;
     s.nx = d.nx;
     s.nz = d.nz;
+    s.pz = r.pz;
+    s.tmap = r.tmaps;
     s.nt = d.nt;
     s.tiles_z = (d.nz + S.tile.tz - 1) / S.tile.tz;
     s.tiles_x = (d.nx + S.tile.tx - 1) / S.tile.tx;
@@ -326,11 +361,11 @@ void fill_slot(const Server &S, const Req &r, Slot &s) {
     s.rinv = r.rinv;
     s.ax = r.ax;
     s.az = r.az;
-    const size_t n = (size_t)d.nx * d.nz;
+    const size_t np = (size_t)d.nx * r.pz;
     if (d.psv)
-        for (int f = 0; f < NPSV; f++) s.psv[f] = r.state + f * n;
+        for (int f = 0; f < NPSV; f++) s.psv[f] = r.state + f * np;
     else
-        for (int f = 0; f < NSH; f++) s.sh[f] = r.state + f * n;
+        for (int f = 0; f < NSH; f++) s.sh[f] = r.state + f * np;
     s.nsfe = r.nsfe;
     s.nf = r.nf;
     s.ckpt_prec = S.prec;
@@ -434,7 +469,7 @@ int round_once(Server &S, std::vector<Req *> &act) {
                 GB_CUDA_TRY(launch_ckpt_store(tab, cnt, (int)max_n_fwd[w], k, 1, w, S.st));
                 S.launches += q16 ? 2 : 1;
             }
-            GB_CUDA_TRY(launch_step(w, S.tile, tab, cnt, max_tiles[w], k, false, S.st));
+            GB_CUDA_TRY(launch_step(w, S.tile, tab, cnt, max_tiles[w], k, S.use_tma(), S.st));
             S.launches++;
             if (k == S.sfe - 1 && cnt > nadj) {
                 if (q16) GB_CUDA_TRY(launch_ckpt_amax(tab, cnt, (int)max_n_fwd[w], k, 0, w, S.st));
@@ -488,6 +523,10 @@ int gb_server_set_option(gb_server *h, const char *key, double value) {
             return GB_ERR_ARG;
         }
         h->s.tile = tile_config(t);
+        return GB_OK;
+    }
+    if (k == "tma") {
+        h->s.opt_tma = value != 0;
         return GB_OK;
     }
     set_error("gb_server_set_option: unknown option " + k);
@@ -577,7 +616,7 @@ int gb_server_run(gb_server *h) {
                 std::vector<double> v(ntr);
                 if (ntr)
                     GB_CUDA_TRY(cudaMemcpyAsync(v.data(), r->val, ntr * 8, cudaMemcpyDeviceToHost, S.st));
-                GB_CUDA_TRY(cudaMemsetAsync(r->state, 0, (size_t)(d.psv ? NPSV : NSH) * n * 4, S.st));
+                GB_CUDA_TRY(cudaMemsetAsync(r->state, 0, (size_t)(d.psv ? NPSV : NSH) * d.nx * r->pz * 4, S.st));
                 GB_CUDA_TRY(cudaStreamSynchronize(S.st));
                 r->misfit = 0;
                 for (double x : v) r->misfit += x;
@@ -604,6 +643,10 @@ int gb_server_run(gb_server *h) {
     }
     GB_CUDA_TRY(cudaStreamSynchronize(S.st));
     S.run_s = now_s(t0);
+    if (S.opt_tma && S.tile.threads > 0 && march_tma_error()) {
+        set_error("server: a bulk-load wait of the marching kernel ran out of iterations; results are invalid");
+        return GB_ERR_CUDA;
+    }
     return GB_OK;
 }
 

@@ -447,12 +447,13 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 // One field float[nx*nz] (k = i*nz + j) as a 2-D tensor {nz, nx}: a box is
 // `rows` consecutive rows of TMAP_BOX_COLS consecutive columns, zero outside
 // the grid.
-static bool encode_field_map(void *out, const float *base, int nx, int nz, int rows) {
+static bool encode_field_map(void *out, const float *base, int nx, int nz, int pz, int rows) {
     const auto enc = tensor_map_encoder();
-    if (!enc || !base || (reinterpret_cast<uintptr_t>(base) & 15) || nz % 4 || rows < 1 || rows > 256 || rows % 4)
+    if (!enc || !base || (reinterpret_cast<uintptr_t>(base) & 15) || pz % 4 || pz < nz || rows < 1 || rows > 256 ||
+        rows % 4)
         return false;
     const cuuint64_t dims[2] = {(cuuint64_t)nz, (cuuint64_t)nx};
-    const cuuint64_t strides[1] = {(cuuint64_t)nz * 4};
+    const cuuint64_t strides[1] = {(cuuint64_t)pz * 4};
     const cuuint32_t box[2] = {(cuuint32_t)rows, (cuuint32_t)TMAP_BOX_COLS};
     const cuuint32_t estr[2] = {1, 1};
     return enc(static_cast<CUtensorMap *>(out), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(base), dims,
@@ -460,30 +461,33 @@ static bool encode_field_map(void *out, const float *base, int nx, int nz, int r
                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-// Encodes the TMAP_N maps of a slot's state fields and the model for a box
-// of `rows` rows; false when a field cannot be described.
-static bool encode_slot_maps(std::vector<CUtensorMap> &h, const float *state, bool sh, bool psv, const float *rinv,
-                             const float *mu, const float *lambda, int nx, int nz, int rows) {
+// Encodes the TMAP_N maps of a slot's state fields and the model (arrays of
+// nx columns at pitch pz) for a box of `rows` rows into h (TMAP_N * TMAP_BYTES
+// bytes); false when a field cannot be described. lambda may be null (SH).
+bool encode_slot_maps(void *h, const float *state, bool sh, bool psv, const float *rinv, const float *mu,
+                      const float *lambda, int nx, int nz, int pz, int rows) {
     static_assert(sizeof(CUtensorMap) == TMAP_BYTES, "tensor map size");
-    h.assign(TMAP_N, CUtensorMap{});
-    const size_t nc = (size_t)nx * nz;
+    CUtensorMap *m = static_cast<CUtensorMap *>(h);
+    for (int q = 0; q < TMAP_N; q++) m[q] = CUtensorMap{};
+    const size_t nc = (size_t)nx * pz;
     bool ok = true;
     const float *p = state;
     if (sh)
-        for (int f = 0; f < NSH; f++) ok = ok && encode_field_map(&h[TMAP_SH + f], p + (size_t)f * nc, nx, nz, rows);
+        for (int f = 0; f < NSH; f++) ok = ok && encode_field_map(&m[TMAP_SH + f], p + (size_t)f * nc, nx, nz, pz, rows);
     if (sh) p += (size_t)NSH * nc;
     if (psv)
-        for (int f = 0; f < NPSV; f++) ok = ok && encode_field_map(&h[f], p + (size_t)f * nc, nx, nz, rows);
-    return ok && encode_field_map(&h[TMAP_RINV], rinv, nx, nz, rows) &&
-           encode_field_map(&h[TMAP_MU], mu, nx, nz, rows) && encode_field_map(&h[TMAP_LAM], lambda, nx, nz, rows);
+        for (int f = 0; f < NPSV; f++) ok = ok && encode_field_map(&m[f], p + (size_t)f * nc, nx, nz, pz, rows);
+    return ok && encode_field_map(&m[TMAP_RINV], rinv, nx, nz, pz, rows) &&
+           encode_field_map(&m[TMAP_MU], mu, nx, nz, pz, rows) &&
+           (!psv || encode_field_map(&m[TMAP_LAM], lambda, nx, nz, pz, rows));
 }
 
 // Space for a slot's tensor maps, for the marching kernel's bulk loads;
 // tma_ok records whether its fields can be described (nz % 4 == 0, aligned
 // buffers, driver support). The maps are encoded by refresh_tmaps.
 int Solver::build_tmaps(SlotBuf &b) {
-    std::vector<CUtensorMap> h;
-    if (!(nz % 4 == 0 && encode_slot_maps(h, b.state, sh, psv, rinv, mu, lambda, nx, nz, 32))) {
+    std::vector<CUtensorMap> h(TMAP_N);
+    if (!(nz % 4 == 0 && encode_slot_maps(h.data(), b.state, sh, psv, rinv, mu, lambda, nx, nz, nz, 32))) {
         tma_ok = false;
         return GB_OK;
     }
@@ -497,9 +501,9 @@ int Solver::build_tmaps(SlotBuf &b) {
 // previous ones. A no-op when they are current or bulk loads are off.
 int Solver::refresh_tmaps(int threads) {
     if (!use_tma() || threads <= 0 || threads == tmaps_T) return GB_OK;
-    std::vector<CUtensorMap> h;
+    std::vector<CUtensorMap> h(TMAP_N);
     for (auto &b : slots) {
-        if (!b.tmaps || !encode_slot_maps(h, b.state, sh, psv, rinv, mu, lambda, nx, nz, threads)) {
+        if (!b.tmaps || !encode_slot_maps(h.data(), b.state, sh, psv, rinv, mu, lambda, nx, nz, nz, threads)) {
             set_error("tensor maps: a field cannot be described for bulk loads");
             return GB_ERR_STATE;
         }
@@ -625,6 +629,7 @@ int Solver::fill_slots(int kind, const int *shots, int n, bool record_u) {
         const SlotBuf &B = slots[b];
         S.nx = nx;
         S.nz = nz;
+        S.pz = nz;
         S.nt = nt;
         S.tiles_z = (nz + tile.tz - 1) / tile.tz;
         S.tiles_x = (nx + tile.tx - 1) / tile.tx;

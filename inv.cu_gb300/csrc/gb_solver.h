@@ -174,6 +174,11 @@ struct Solver {
     int max_tiles() const { return ((nz + tile.tz - 1) / tile.tz) * ((nx + tile.tx - 1) / tile.tx); }
 };
 
+// Tensor maps of a slot's fields for the marching kernel's bulk loads
+// (gb_solver.cu): TMAP_N maps into h, for arrays of nx columns at pitch pz.
+bool encode_slot_maps(void *h, const float *state, bool sh, bool psv, const float *rinv, const float *mu,
+                      const float *lambda, int nx, int nz, int pz, int rows);
+
 }  // namespace gb
 
 struct gb_solver {

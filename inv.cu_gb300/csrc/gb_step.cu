@@ -423,17 +423,25 @@ __device__ __forceinline__ CkGroup ckpt_group(const Slot &S, bool psv, int which
 // Field f of group g at cell k, in FP32: a copy, or the forward-staggered
 // differences of the kernel accumulation (the guards and arithmetic of
 // k_interaction's FP32 path: 0 where the reference skips a difference).
+// The state address of reference-layout cell k (i*nz + j) at the slot's pitch.
+__device__ __forceinline__ size_t state_addr(const Slot &S, size_t k) {
+    if (S.pz == S.nz) return k;
+    const size_t i = k / S.nz;
+    return i * S.pz + (k - i * S.nz);
+}
+
 __device__ __forceinline__ float ckpt_value(const Slot &S, const CkGroup &g, int f, size_t k) {
-    if (g.kind == 0) return __ldg((f == 0 ? g.a : g.b) + k);
-    const int nx = S.nx, nz = S.nz;
+    const size_t a = state_addr(S, k);
+    if (g.kind == 0) return __ldg((f == 0 ? g.a : g.b) + a);
+    const int nx = S.nx, nz = S.nz, pz = S.pz;
     const int i = (int)(k / nz), j = (int)(k - (size_t)i * nz);
     const bool gx = i >= 1 && i < nx - 2, gz = j >= 1 && j < nz - 2;
     auto ddx = [&](const float *w) {
-        return gx ? dplus(__ldg(w + k + nz), __ldg(w + k), __ldg(w + k + 2 * nz), __ldg(w + k - nz), S.c9x, S.c24x)
+        return gx ? dplus(__ldg(w + a + pz), __ldg(w + a), __ldg(w + a + 2 * pz), __ldg(w + a - pz), S.c9x, S.c24x)
                   : 0.f;
     };
     auto ddz = [&](const float *w) {
-        return gz ? dplus(__ldg(w + k + 1), __ldg(w + k), __ldg(w + k + 2), __ldg(w + k - 1), S.c9z, S.c24z) : 0.f;
+        return gz ? dplus(__ldg(w + a + 1), __ldg(w + a), __ldg(w + a + 2), __ldg(w + a - 1), S.c9z, S.c24z) : 0.f;
     };
     if (g.kind == 1) return f == 0 ? ddx(g.a) : ddz(g.a);
     if (f == 2) return ddx(g.b) + ddz(g.a);  // d(uz)/dx + d(ux)/dz, summed as st_kmu_psv sums them
@@ -573,9 +581,12 @@ __global__ void k_interaction(const Slot *__restrict__ slots, const KernelGroup 
             const float a = S.ckpt_amax ? S.ckpt_amax[(size_t)isfe * S.nf + base + q] : 0.f;
             inv[q] = 1.f / ckpt_scale(a, S.ckpt_prec);
         }
+        // the slot's state at its pitch; checkpoints and kernels in the reference layout
+        const int pz = S.pz;
+        const size_t a = (size_t)i * pz + j;
         auto grad = [&](const float *w, float &ddx, float &ddz) {
-            ddx = gx ? dplus(__ldg(w + k + nz), __ldg(w + k), __ldg(w + k + 2 * nz), __ldg(w + k - nz), c9x, c24x) : 0.f;
-            ddz = gz ? dplus(__ldg(w + k + 1), __ldg(w + k), __ldg(w + k + 2), __ldg(w + k - 1), c9z, c24z) : 0.f;
+            ddx = gx ? dplus(__ldg(w + a + pz), __ldg(w + a), __ldg(w + a + 2 * pz), __ldg(w + a - pz), c9x, c24x) : 0.f;
+            ddz = gz ? dplus(__ldg(w + a + 1), __ldg(w + a), __ldg(w + a + 2), __ldg(w + a - 1), c9z, c24z) : 0.f;
         };
         auto grad_ck = [&](int q, float &ddx, float &ddz) {
             const float iv = inv[q];
@@ -607,7 +618,7 @@ __global__ void k_interaction(const Slot *__restrict__ slots, const KernelGroup 
             if (G.inv_rho) {
                 const float vx_fw = ck(q16 ? 3 : 2);
                 const float vz_fw = ck(q16 ? 4 : 3);
-                kr = st_krho_psv(kr, vx_fw, __ldg(S.psv[VX0 + par] + k), vz_fw, __ldg(S.psv[VZ0 + par] + k), ndt);
+                kr = st_krho_psv(kr, vx_fw, __ldg(S.psv[VX0 + par] + a), vz_fw, __ldg(S.psv[VZ0 + par] + a), ndt);
             }
             if (G.inv_mu)
                 km = q16 ? st_kmu_psv_strain(km, dvxdx, dvxdz, dvzdx, dvzdz, fdv, fdd, fsh, ndt)
@@ -626,7 +637,7 @@ __global__ void k_interaction(const Slot *__restrict__ slots, const KernelGroup 
             }
             if (G.inv_rho) {
                 const float vy_fw = ck(q16 ? 2 : 1);
-                kr = st_krho_sh(kr, vy_fw, __ldg(S.sh[VY0 + par] + k), ndt);
+                kr = st_krho_sh(kr, vy_fw, __ldg(S.sh[VY0 + par] + a), ndt);
             }
             if (G.inv_mu) km = st_kmu_sh(km, dvydx, fdx, dvydz, fdz, ndt);
         }

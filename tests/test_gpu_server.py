@@ -86,3 +86,45 @@ def test_admission_waits_for_memory(gpu):
     assert free.stats().max_concurrent == 4
     for a, b in zip(ids, fid):
         np.testing.assert_array_equal(srv.result(a)["k_mu"], free.result(b)["k_mu"])
+
+
+def test_bulk_loads_and_pitch_identical_to_per_row_loads(gpu):
+    """Requests of any nz are stored at a pitch of nz rounded up to a
+    multiple of 4 so that the marching kernel can load their columns with
+    bulk tensor copies: the kernels and misfits are bit-identical to those
+    of per-row cp.async loads (pitch unchanged there as well), and to the
+    2-D tile kernel's, which keeps the reference layout."""
+    mix = MIX + [(1, 77, 61, 200, 7), (0, 95, 33, 200, 8)]
+    reqs = [request(*m)[1] for m in mix]
+    out = []
+    for opts in ({}, {"tma": 0}, {"tile": 3}):
+        srv = gpu.Server(sfe=10)
+        for k, v in opts.items():
+            srv.set_option(k, v)
+        ids = [srv.submit(arrival=0.0, **r) for r in reqs]
+        srv.run()
+        out.append([srv.result(i) for i in ids])
+    for other in out[1:]:
+        for a, b in zip(out[0], other):
+            for name in ("k_lambda", "k_mu", "k_rho"):
+                np.testing.assert_array_equal(a[name], b[name])
+            assert a["misfit"] == b["misfit"]
+
+
+def test_served_request_with_odd_nz_matches_oracle(gpu, orc):
+    case, req = request(1, 83, 69, 200, 13)
+    pb = cases.oracle_problem(orc, case)
+    rng = np.random.default_rng(6)
+    obs = {c: (rng.standard_normal((pb.nrec, pb.nt)) * 1e-9).astype(np.float32) for c in "xz"}
+    srv = gpu.Server(sfe=10)
+    rid = srv.submit(obs=np.stack([obs[c] for c in "xz"]), **req)
+    srv.run()
+    res = srv.result(rid)
+    o = orc.forward(pb, 0, adj=True)
+    tw = orc.taper(pb.nt, case["dt"])
+    ad = {c: np.zeros((pb.nrec, pb.nt), np.float32) for c in "xyz"}
+    for c in "xz":
+        _, ad[c] = orc.waveform_misfit(o["xyz".index(c)], obs[c], tw, case["dt"])
+    kern = orc.adjoint(pb, [ad["x"], ad["y"], ad["z"]], o[3])
+    for q, name in enumerate(("k_lambda", "k_mu", "k_rho")):
+        assert cases.rel(res[name], kern[q]) < 1e-4, name
