@@ -324,7 +324,7 @@ typedef struct {
 } gb_server_stats;
 gb_server *gb_server_create(int sfe, int ckpt_precision, double hbm_budget_gb, int max_slots);
 /* Options, set before gb_server_run: "tile" (step kernel configuration 1..20,
- * as gb_solver_set_option; default 11, marching strips of 152 rows), "tma"
+ * as gb_solver_set_option; default 9, marching strips of 120 rows), "tma"
  * (1: the marching kernel loads grid columns with bulk tensor copies, each
  * request's arrays stored at a pitch of nz rounded up to a multiple of 4,
  * default; 0: per-row cp.async; the results are the same). */

