@@ -672,12 +672,41 @@ def run_c4(args):
     one = serve(np.zeros(seq), max_slots=1, tile=3) if seq > 0 else None
     cu_sat = sat.cell_updates / sat.wall_s
     cu_seq = sum(cells[:seq]) / one.wall_s if one else None
+    # the plain path: each request through its own solver, one shot per call,
+    # one fused step launch per time step, FP32 checkpoints, no CUDA graphs,
+    # no cluster pass (solver created, model uploaded and gradient run per
+    # request, as a caller without the engine would)
+    plain = None
+    npl = min(nreq, args.sequential)
+    if npl > 0:
+        tmp = tempfile.mkdtemp(prefix="gbfwi_c4_")
+        t0 = time.perf_counter()
+        for r in reqs[:npl]:
+            vals = {"mode": 2, "sh": 1 - r["psv"], "psv": r["psv"], "nt": r["nt"], "dt": r["dt"], "sfe": 10,
+                    "model_type": 0, "trace_type": 0, "abs_left": 1, "abs_right": 1, "abs_bottom": 1, "abs_top": 0,
+                    "abs_width": 20, "abs_alpha": 0.015, "inv_lambda": 1, "inv_mu": 1, "inv_rho": 1,
+                    "batch": 1, "graphs": 0, "cluster": 0, "ckpt_precision": 0}
+            cfg = pkg.Config.new(tmp, vals, [r["src"]], r["rec"].tolist())
+            sol = pkg.FdmSolver(cfg, grid=(r["nx"], r["nz"], (r["nx"] - 1) * r["dx"], (r["nz"] - 1) * r["dx"]))
+            sol.set_model_grid(r["lam"], r["mu"], r["rho"])
+            comps = "xz" if r["psv"] else "y"
+            mis = pkg.Misfit.from_obs(0, sol, {c: np.zeros((1, len(r["rec"]), r["nt"]), np.float32) for c in comps})
+            mis.run(kernel=True)
+            mis.close()
+            sol.close()
+            del cfg
+        wall = time.perf_counter() - t0
+        plain = {"requests": npl, "wall_s": round(wall, 2), "requests_per_s": round(npl / wall, 3),
+                 "cell_updates_per_s": round(sum(cells[:npl]) / wall, 1),
+                 "what": "each request through its own solver: one shot per call, one fused step launch per "
+                         "time step, FP32 checkpoints, no CUDA graphs, no cluster pass"}
     _line("served forward+adjoint requests/s", round(cap, 3), "requests/s",
           {"workload": "%d requests, 50/50 P-SV/SH, sides U[128,1024] at 10 m, 1000-5000 steps (dt 0.8 ms), "
                        "layered faulted models, FP16 checkpoints" % nreq},
           capacity={"requests_per_s": round(cap, 3), "cell_updates_per_s": round(cu_sat, 1),
                     "wall_s": round(sat.wall_s, 2), "max_concurrent": sat.max_concurrent,
                     "over_sequential_cell_updates": round(cu_sat / cu_seq, 2) if cu_seq else None,
+                    "over_plain_path_cell_updates": round(cu_sat / plain["cell_updates_per_s"], 2) if plain else None,
                     "launches": int(sat.launches), "rounds": int(sat.rounds)},
           under_load=None if live is None else {
               "arrival_rate_per_s": round(rate, 3), "fraction_of_capacity": round(rate / cap, 3),
@@ -687,6 +716,7 @@ def run_c4(args):
           sequential=None if one is None else {
               "requests": seq, "wall_s": round(one.wall_s, 2), "requests_per_s": round(seq / one.wall_s, 3),
               "cell_updates_per_s": round(cu_seq, 1), "p50_latency_s_one_at_a_time": round(one.p50_s, 3)},
+          plain_path=plain,
           gpu_launches=int(sat.launches))
 
 

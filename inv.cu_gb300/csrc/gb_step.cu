@@ -430,9 +430,17 @@ __device__ __forceinline__ size_t state_addr(const Slot &S, size_t k) {
     return i * S.pz + (k - i * S.nz);
 }
 
-__device__ __forceinline__ float ckpt_value(const Slot &S, const CkGroup &g, int f, size_t k) {
+// Every field of group g at cell k, in FP32: copies, or the forward-staggered
+// differences of the kernel accumulation (the guards and arithmetic of
+// k_interaction's FP32 path: 0 where the reference skips a difference), each
+// neighbour loaded once for all the group's fields.
+__device__ __forceinline__ void ckpt_values(const Slot &S, const CkGroup &g, size_t k, float *out) {
     const size_t a = state_addr(S, k);
-    if (g.kind == 0) return __ldg((f == 0 ? g.a : g.b) + a);
+    if (g.kind == 0) {
+        out[0] = __ldg(g.a + a);
+        if (g.nfld > 1) out[1] = __ldg(g.b + a);
+        return;
+    }
     const int nx = S.nx, nz = S.nz, pz = S.pz;
     const int i = (int)(k / nz), j = (int)(k - (size_t)i * nz);
     const bool gx = i >= 1 && i < nx - 2, gz = j >= 1 && j < nz - 2;
@@ -443,10 +451,15 @@ __device__ __forceinline__ float ckpt_value(const Slot &S, const CkGroup &g, int
     auto ddz = [&](const float *w) {
         return gz ? dplus(__ldg(w + a + 1), __ldg(w + a), __ldg(w + a + 2), __ldg(w + a - 1), S.c9z, S.c24z) : 0.f;
     };
-    if (g.kind == 1) return f == 0 ? ddx(g.a) : ddz(g.a);
-    if (f == 2) return ddx(g.b) + ddz(g.a);  // d(uz)/dx + d(ux)/dz, summed as st_kmu_psv sums them
+    if (g.kind == 1) {
+        out[0] = ddx(g.a);
+        out[1] = ddz(g.a);
+        return;
+    }
     const float exx = ddx(g.a), ezz = ddz(g.b);
-    return f == 0 ? exx + ezz : exx - ezz;  // divergence, normal-strain difference
+    out[0] = exx + ezz;              // divergence
+    out[1] = exx - ezz;              // normal-strain difference
+    out[2] = ddx(g.b) + ddz(g.a);    // d(uz)/dx + d(ux)/dz, summed as st_kmu_psv sums them
 }
 
 // Checkpoint slot of step index k for slot S, or -1 when k is not a
@@ -470,21 +483,29 @@ __global__ void k_ckpt_amax(const Slot *__restrict__ slots, int kstep, int which
     const CkGroup g = ckpt_group(S, psv, which_u, par);
     const size_t n = (size_t)S.nx * S.nz;
     __shared__ float red[3][32];
-    for (int f = 0; f < g.nfld; f++) {
-        float m = 0.f;
-        for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
-            m = fmaxf(m, fabsf(ckpt_value(S, g, f, k)));
-        for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-        if ((threadIdx.x & 31) == 0) red[f][threadIdx.x >> 5] = m;
+    float m[3] = {0.f, 0.f, 0.f};
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+        float v[3];
+        ckpt_values(S, g, k, v);
+#pragma unroll
+        for (int f = 0; f < 3; f++)
+            if (f < g.nfld) m[f] = fmaxf(m[f], fabsf(v[f]));
+    }
+#pragma unroll
+    for (int f = 0; f < 3; f++) {
+        if (f >= g.nfld) break;
+        float x = m[f];
+        for (int o = 16; o; o >>= 1) x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, o));
+        if ((threadIdx.x & 31) == 0) red[f][threadIdx.x >> 5] = x;
     }
     __syncthreads();
     if (threadIdx.x < 32) {
         for (int f = 0; f < g.nfld; f++) {
-            float m = threadIdx.x < (blockDim.x >> 5) ? red[f][threadIdx.x] : 0.f;
-            for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+            float x = threadIdx.x < (blockDim.x >> 5) ? red[f][threadIdx.x] : 0.f;
+            for (int o = 16; o; o >>= 1) x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, o));
             // non-negative floats order like their bit patterns
             if (threadIdx.x == 0)
-                atomicMax(reinterpret_cast<unsigned *>(S.ckpt_amax) + (size_t)isfe * S.nf + g.q[f], __float_as_uint(m));
+                atomicMax(reinterpret_cast<unsigned *>(S.ckpt_amax) + (size_t)isfe * S.nf + g.q[f], __float_as_uint(x));
         }
     }
 }
@@ -497,23 +518,26 @@ __global__ void k_ckpt_store(const Slot *__restrict__ slots, int kstep, int whic
     if (psv ? S.psv[0] == nullptr : S.sh[0] == nullptr) return;
     const CkGroup g = ckpt_group(S, psv, which_u, par);
     const size_t n = (size_t)S.nx * S.nz;
-    for (int f = 0; f < g.nfld; f++) {
-        const size_t off = ((size_t)isfe * S.nf + g.q[f]) * n;
-        if (S.ckpt_prec == CKPT_F32) {
-            float *dst = static_cast<float *>(S.ckpt) + off;
-            for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
-                dst[k] = ckpt_value(S, g, f, k);
-        } else {
-            const float sc = ckpt_scale(S.ckpt_amax[(size_t)isfe * S.nf + g.q[f]], S.ckpt_prec);
-            if (S.ckpt_prec == CKPT_BF16) {
-                __nv_bfloat16 *dst = static_cast<__nv_bfloat16 *>(S.ckpt) + off;
-                for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
-                    dst[k] = __float2bfloat16_rn(ckpt_value(S, g, f, k) * sc);
-            } else {
-                __half *dst = static_cast<__half *>(S.ckpt) + off;
-                for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
-                    dst[k] = __float2half_rn(ckpt_value(S, g, f, k) * sc);
-            }
+    size_t off[3];
+    float sc[3] = {1.f, 1.f, 1.f};
+#pragma unroll
+    for (int f = 0; f < 3; f++) {
+        off[f] = ((size_t)isfe * S.nf + g.q[f < g.nfld ? f : 0]) * n;
+        if (f >= g.nfld) continue;
+        if (S.ckpt_prec != CKPT_F32) sc[f] = ckpt_scale(S.ckpt_amax[(size_t)isfe * S.nf + g.q[f]], S.ckpt_prec);
+    }
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+        float v[3];
+        ckpt_values(S, g, k, v);
+#pragma unroll
+        for (int f = 0; f < 3; f++) {
+            if (f >= g.nfld) break;
+            if (S.ckpt_prec == CKPT_F32)
+                static_cast<float *>(S.ckpt)[off[f] + k] = v[f];
+            else if (S.ckpt_prec == CKPT_BF16)
+                static_cast<__nv_bfloat16 *>(S.ckpt)[off[f] + k] = __float2bfloat16_rn(v[f] * sc[f]);
+            else
+                static_cast<__half *>(S.ckpt)[off[f] + k] = __float2half_rn(v[f] * sc[f]);
         }
     }
 }
