@@ -22,6 +22,8 @@
 //
 // Arithmetic, guards and update order are those of the 2-D tile kernel
 // (solver/fdm.h:76-161): results do not depend on T, C or batching.
+#include <type_traits>
+
 #include "gb_internal.h"
 #include "gb_stencil.h"
 
@@ -131,8 +133,12 @@ __host__ __device__ constexpr int march_smem_words(int threads) {
 // per field and 32 rows) that complete on the ring slot's mbarrier; needs
 // nz % 4 == 0 and the slots' tensor maps. Both read the same values for
 // every cell they use, so results are identical.
+// Registers are capped per wave system (SH 96, P-SV 128, no spills): left to
+// itself ptxas settled the SH form at 64-80 registers with spills, and the
+// 16-shot 4096 x 1024 steps ran fastest with these caps (higher ones leave
+// fewer blocks resident).
 template <bool PSV, bool TMA>
-__global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restrict__ slots, int kstep,
+__global__ void __maxnreg__(PSV ? 128 : 96) k_march(const Slot *__restrict__ slots, int kstep,
                                                             int chunk) {
     using W = MarchWords<PSV>;
     constexpr int NS = W::NS, NV = W::NV;
@@ -204,7 +210,7 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
         v_out[0] = S.sh[VY0 + (par ^ 1)];
         u[0] = S.sh[UY];
     }
-    const float *lam = S.lambda, *mu = S.mu, *rinv_g = S.rinv, *ax = S.ax;
+    const float *lam = S.lambda, *mu = S.mu, *rinv_g = S.rinv;
 
     // Sources in the velocity region of this window and receivers of its
     // owned cells, both sorted by column then row. The next entry's cell is
@@ -410,45 +416,40 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
             cpa_commit();
         }
     }
-    // P-SV: unrolled by the queue depth, so the register queues rotate by
-    // renaming (fewer registers and moves); SH keeps the rolled loop, which
-    // fits its registers better
-    constexpr int kUnroll = PSV ? 4 : 1;
-#pragma unroll kUnroll
-    for (int q = 0; q < nstep; q++) {
+    // bulk loads: waits for stage m (whole strip, kStageCols columns; phase
+    // m / kStages of its barrier) and refills the ring stage consumed in
+    // stage m-1 (every thread finished reading it before the previous column
+    // step's barrier); returns the stage's ring row of this thread
+    auto stage_start = [&](int m) -> const float * {
+        if (!dead && !mbar_wait_bounded(bar0 + 8u * (unsigned)(m % kStages), (unsigned)((m / kStages) & 1))) {
+            dead = true;
+            s_dead = 1;
+            atomicOr(&g_march_tma_error, 1);
+        }
+        sdone = m + 1;
+        if (m >= 1 && m + 1 < nstage && !dead) {
+            issue_tma(m + 1);
+            issued = m + 2;
+        }
+        return ring + (m % kStages) * W::N * kStageCols * T + t;
+    };
+    // word stride of a column step in the ring
+    const int ws = TMA ? kStageCols * T : T;
+
+    // Column step q: the stress of column p = p_first + q arrives (ring row
+    // rs), the velocity and displacement of column p - 1 and the stress of
+    // column p - 3 are updated. STEADY: a step whose velocity column is
+    // stored and whose stress column is updated, in a chunk at least two
+    // columns away from the grid's x edges, where every column test below
+    // holds and is left out. CHK: read the block's bulk-load failure flag
+    // after the barrier (it can only be set at a stage's first step).
+    // Returns false when the march must stop (a bulk-load wait failed).
+    auto step = [&](const int q, const float *rs, auto steady, const bool chk) __attribute__((always_inline)) {
+        constexpr bool STEADY = decltype(steady)::value;
         const int p = p_first + q;
         float cur[W::N];
-        if (TMA) {
-            const int m = q / kStageCols, qc = q - m * kStageCols;
-            if (qc == 0) {
-                // stage m has landed (whole strip, kStageCols columns): phase m / kStages of its barrier
-                if (!dead && !mbar_wait_bounded(bar0 + 8u * (unsigned)(m % kStages), (unsigned)((m / kStages) & 1))) {
-                    dead = true;
-                    s_dead = 1;
-                    atomicOr(&g_march_tma_error, 1);
-                }
-                sdone = m + 1;
-                // refill the stage consumed in stage m-1 (every thread finished
-                // reading it before the previous column step's barrier)
-                if (m >= 1 && m + 1 < nstage && !dead) {
-                    issue_tma(m + 1);
-                    issued = m + 2;
-                }
-            }
-            const float *rs = ring + ((m % kStages) * W::N * kStageCols + qc) * T + t;
 #pragma unroll
-            for (int w = 0; w < W::N; w++) cur[w] = rs[w * kStageCols * T];
-        } else {
-            cpa_wait<kRing - 2>();  // column step q has landed (own row)
-            const float *rs = ring + (q % kRing) * W::N * T + t;
-#pragma unroll
-            for (int w = 0; w < W::N; w++) cur[w] = rs[w * T];
-            // refill the slot read at the previous step (every thread finished
-            // reading it before the previous step's barrier)
-            if (q + kRing - 1 < nstep) issue(p + kRing - 1, (q + kRing - 1) % kRing);
-            cpa_commit();
-        }
-
+        for (int w = 0; w < W::N; w++) cur[w] = rs[w * ws];
         const int buf = q & 1;
 #pragma unroll
         for (int f = 0; f < NS; f++) {
@@ -465,14 +466,14 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
             sz_w[st] = cur[W::SG + 1];  // szy
         }
         const int pv = p - 1;  // velocity column of this step
-        const bool vcol = pv >= c0 - 1;
+        const bool vcol = STEADY || pv >= c0 - 1;
         float vn[NV];
 #pragma unroll
         for (int f = 0; f < NV; f++) vn[f] = 0.f;
         if (vcol) {
             const float *sz_r = s_sz + (buf ^ 1) * NZS * TP;
             float ds[NV];
-            const bool xS = pv >= 2 && pv < nx - 2;
+            const bool xS = STEADY || (pv >= 2 && pv < nx - 2);
             if (PSV) {
                 float dsx = xS ? dminus_m(sq[2][0], sq[1][0], sq[3][0], sq[0][0], c9x, c24x) : 0.f;
                 float dsz = xS ? dminus_m(sq[2][2], sq[1][2], sq[3][2], sq[0][2], c9x, c24x) : 0.f;
@@ -515,13 +516,17 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
                 inj_ptr++;
                 inj_next = inj_ptr < inj_end ? inj_local[inj_ptr] : 0x7fffffff;
             }
-            if ((unsigned)pv < (unsigned)nx && rowin) {
+            if (STEADY || ((unsigned)pv < (unsigned)nx && rowin)) {
                 const float ab = ax_stage()[pv - (c0 - 1)] * azj;
                 const float rinv = cur[W::RHO];
 #pragma unroll
-                for (int f = 0; f < NV; f++) vn[f] = st_velocity(ab, dt, ds[f], rinv, cur[W::V + f]);
+                for (int f = 0; f < NV; f++) {
+                    vn[f] = st_velocity(ab, dt, ds[f], rinv, cur[W::V + f]);
+                    // rows outside the grid keep 0, as in the other steps
+                    if (STEADY) vn[f] = rowin ? vn[f] : 0.f;
+                }
             }
-            if (pv >= c0 && pv < c1) {
+            if (STEADY || (pv >= c0 && pv < c1)) {
                 const int oc = pv - c0;
                 float un[NV];
 #pragma unroll
@@ -562,7 +567,7 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
             vz_w[f * TP + st] = vn[f];
         }
         __syncthreads();
-        if (TMA && s_dead) break;  // uniform: s_dead is read after the barrier
+        if (TMA && chk && s_dead) return false;  // uniform: s_dead is read after the barrier
         // z-gradient of the new velocity at column pv
 #pragma unroll
         for (int f = 0; f < NV; f++) {
@@ -573,8 +578,8 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
         }
         // stress update at column pm = p - 3 (solver/fdm.h:138-149)
         const int pm = p - 3;
-        if (pm >= c0 && pm < c1 && rowown) {
-            const bool xV = pm >= 1 && pm < nx - 2;
+        if ((STEADY || (pm >= c0 && pm < c1)) && rowown) {
+            const bool xV = STEADY || (pm >= 1 && pm < nx - 2);
             const int km = pm * pz + j;
             const float m = cur[W::MU];
             if (PSV) {
@@ -595,7 +600,57 @@ __global__ void __launch_bounds__(kMaxMarchThreads) k_march(const Slot *__restri
                 sig_out[1][km] = szy;
             }
         }
+        return true;
+    };
+    // any column step, with its ring handling
+    auto any_step = [&](const int q) -> bool {
+        const float *rs;
+        bool chk = false;
+        if (TMA) {
+            const int m = q / kStageCols, qc = q - m * kStageCols;
+            if (qc == 0) {
+                rs = stage_start(m);
+                chk = true;
+            } else {
+                rs = ring + (m % kStages) * W::N * kStageCols * T + t;
+            }
+            rs += qc * T;
+        } else {
+            cpa_wait<kRing - 2>();  // column step q has landed (own row)
+            rs = ring + (q % kRing) * W::N * T + t;
+            // refill the slot read at the previous step (every thread
+            // finished reading it before the previous step's barrier)
+            if (q + kRing - 1 < nstep) issue(p_first + q + kRing - 1, (q + kRing - 1) % kRing);
+            cpa_commit();
+        }
+        return step(q, rs, std::false_type{}, chk);
+    };
+
+    // Steps 0..7 (the velocity and stress columns start at steps 3 and 6),
+    // then, with bulk loads in a chunk away from the grid's x edges, whole
+    // stages of steady steps while the stage's last step stores its velocity
+    // column (q < cc + 4), then the remaining steps.
+    const int cc = c1 - c0;
+    const bool interior = c0 >= 2 && c1 <= nx - 2;
+    constexpr int kSteadyStage = 2;  // first stage whose steps are all past step 6
+    const int m_end = (TMA && interior) ? cc / kStageCols + 1 : 0;
+    bool run = true;
+    int q = 0;
+    for (; q < nstep && q < kSteadyStage * kStageCols && run; q++) run = any_step(q);
+    if (run && m_end > kSteadyStage) {
+        for (int m = kSteadyStage; m < m_end; m++) {
+            const float *rs = stage_start(m);
+            const int q0 = m * kStageCols;
+            if (!step(q0, rs, std::true_type{}, true)) {
+                run = false;
+                break;
+            }
+#pragma unroll
+            for (int qc = 1; qc < kStageCols; qc++) step(q0 + qc, rs + qc * T, std::true_type{}, false);
+        }
+        q = m_end * kStageCols;
     }
+    for (; q < nstep && run; q++) run = any_step(q);
     if (!TMA) cpa_wait<0>();
     if (TMA && s_dead) {
         // leave no bulk copy in flight into this block's shared memory
