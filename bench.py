@@ -647,6 +647,8 @@ def run_c4(args):
         srv = pkg.Server(sfe=10, ckpt=2, max_slots=max_slots)
         if tile:
             srv.set_option("tile", tile)
+        if args.server_streams:
+            srv.set_option("streams", args.server_streams)
         for q, r in enumerate(reqs[:len(arrivals)]):
             srv.submit(arrival=float(arrivals[q]), **r)
         srv.run()
@@ -976,6 +978,8 @@ def main():
     ap.add_argument("--sequential", type=int, default=64, help="c4 requests also solved one at a time")
     ap.add_argument("--server-tile", type=int, default=0,
                     help="c4 step kernel configuration (0: the engine's default)")
+    ap.add_argument("--server-streams", type=int, default=0,
+                    help="c4 engine streams, 1 or 2 (0: the engine's default)")
     ap.add_argument("--profile-case", default="", help="run one small case for an ncu capture")
     ap.add_argument("--tile", type=int, default=3, help="kernel configuration for --profile-case")
     ap.add_argument("--tma", type=int, default=1, help="--profile-case: marching kernel bulk loads (1) or cp.async (0)")

@@ -327,7 +327,9 @@ gb_server *gb_server_create(int sfe, int ckpt_precision, double hbm_budget_gb, i
  * as gb_solver_set_option; default 9, marching strips of 120 rows), "tma"
  * (1: the marching kernel loads grid columns with bulk tensor copies, each
  * request's arrays stored at a pitch of nz rounded up to a multiple of 4,
- * default; 0: per-row cp.async; the results are the same). */
+ * default; 0: per-row cp.async; the results are the same), "streams" (2: the
+ * SH requests' steps of a round run on a second stream beside the P-SV
+ * ones, default; 1: one stream; the results are the same). */
 int gb_server_set_option(gb_server *srv, const char *key, double value);
 /* Queues a request; returns its id (>= 0) or -1. */
 long long gb_server_submit(gb_server *srv, const gb_request_desc *req);

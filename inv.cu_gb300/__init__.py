@@ -603,7 +603,7 @@ class Server:
         self._keep = {}
 
     def set_option(self, key, value):
-        """Engine option set before run(): "tile" (step kernel configuration 1..20), "tma" (0/1)."""
+        """Engine option set before run(): "tile" (step kernel configuration 1..20), "tma" (0/1), "streams" (1/2)."""
         check(lib().gb_server_set_option(self._h, key.encode(), float(value)))
 
     def submit(self, *, psv, nx, nz, dx, dt, nt, lam, mu, rho, src, rec, obs=None, arrival=0.0, abs_width=20,

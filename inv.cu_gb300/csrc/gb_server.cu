@@ -89,6 +89,14 @@ struct Server {
     double budget = 0;
     size_t used = 0;
     cudaStream_t st = nullptr;
+    // SH steps of a round run on st2 beside the P-SV steps on st (option
+    // "streams" 2): the wave systems' requests are independent within a
+    // round, and each chain fills the other's launch tails. st2 starts after
+    // the round's table copy (ev_fork) and st waits for it at the round's end
+    // (ev_join).
+    int streams = 2;
+    cudaStream_t st2 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     std::vector<Req> reqs;
     // Slot and group tables: one device copy, and a ring of pinned host
     // staging buffers; a staging buffer is refilled only after the event
@@ -459,31 +467,47 @@ int round_once(Server &S, std::vector<Req *> &act) {
     const int base_psv = 0, n_psv = counts[1][0] + counts[1][1];
     const int base_sh = n_psv, n_sh = counts[0][0] + counts[0][1];
     const bool q16 = S.prec != CKPT_F32;
+    // the SH chain on its own stream when both systems have requests
+    const bool fork = S.streams > 1 && n_psv > 0 && n_sh > 0;
+    if (fork) {
+        if (!S.st2) {
+            GB_CUDA_TRY(cudaStreamCreateWithFlags(&S.st2, cudaStreamNonBlocking));
+            GB_CUDA_TRY(cudaEventCreateWithFlags(&S.ev_fork, cudaEventDisableTiming));
+            GB_CUDA_TRY(cudaEventCreateWithFlags(&S.ev_join, cudaEventDisableTiming));
+        }
+        GB_CUDA_TRY(cudaEventRecord(S.ev_fork, S.st));
+        GB_CUDA_TRY(cudaStreamWaitEvent(S.st2, S.ev_fork, 0));
+    }
     for (int k = 0; k < S.sfe; k++) {
         for (int w = 1; w >= 0; w--) {
             const int base = w ? base_psv : base_sh, cnt = w ? n_psv : n_sh;
             if (!cnt) continue;
             const int nadj = counts[w][1];
             const Slot *tab = S.d_tab + base;
+            const cudaStream_t sw = (fork && w == 0) ? S.st2 : S.st;
             // forward checkpoints of u before the step (the kernels select
             // the forward slots whose step is a checkpoint step)
             if (k == S.sfe - 1 && cnt > nadj) {
-                if (q16) GB_CUDA_TRY(launch_ckpt_amax(tab, cnt, (int)max_n_fwd[w], k, 1, w, S.st));
-                GB_CUDA_TRY(launch_ckpt_store(tab, cnt, (int)max_n_fwd[w], k, 1, w, S.st));
+                if (q16) GB_CUDA_TRY(launch_ckpt_amax(tab, cnt, (int)max_n_fwd[w], k, 1, w, sw));
+                GB_CUDA_TRY(launch_ckpt_store(tab, cnt, (int)max_n_fwd[w], k, 1, w, sw));
                 S.launches += q16 ? 2 : 1;
             }
-            GB_CUDA_TRY(launch_step(w, S.tile, tab, cnt, max_tiles[w], k, S.use_tma(), S.st));
+            GB_CUDA_TRY(launch_step(w, S.tile, tab, cnt, max_tiles[w], k, S.use_tma(), sw));
             S.launches++;
             if (k == S.sfe - 1 && cnt > nadj) {
-                if (q16) GB_CUDA_TRY(launch_ckpt_amax(tab, cnt, (int)max_n_fwd[w], k, 0, w, S.st));
-                GB_CUDA_TRY(launch_ckpt_store(tab, cnt, (int)max_n_fwd[w], k, 0, w, S.st));
+                if (q16) GB_CUDA_TRY(launch_ckpt_amax(tab, cnt, (int)max_n_fwd[w], k, 0, w, sw));
+                GB_CUDA_TRY(launch_ckpt_store(tab, cnt, (int)max_n_fwd[w], k, 0, w, sw));
                 S.launches += q16 ? 2 : 1;
             }
             if (k == 0 && nadj) {
-                GB_CUDA_TRY(launch_interaction(w, S.d_tab, S.d_grp + base, nadj, max_cells[w], k, S.st));
+                GB_CUDA_TRY(launch_interaction(w, S.d_tab, S.d_grp + base, nadj, max_cells[w], k, sw));
                 S.launches++;
             }
         }
+    }
+    if (fork) {
+        GB_CUDA_TRY(cudaEventRecord(S.ev_join, S.st2));
+        GB_CUDA_TRY(cudaStreamWaitEvent(S.st, S.ev_join, 0));
     }
     for (Req *r : act) r->it += S.sfe;
     S.rounds++;
@@ -530,6 +554,14 @@ int gb_server_set_option(gb_server *h, const char *key, double value) {
     }
     if (k == "tma") {
         h->s.opt_tma = value != 0;
+        return GB_OK;
+    }
+    if (k == "streams") {
+        if (value != 1 && value != 2) {
+            set_error("gb_server_set_option: streams must be 1 or 2");
+            return GB_ERR_ARG;
+        }
+        h->s.streams = (int)value;
         return GB_OK;
     }
     set_error("gb_server_set_option: unknown option " + k);
@@ -712,6 +744,10 @@ void gb_server_destroy(gb_server *h) {
         cudaFreeHost(S.h_grp[b]);
         if (S.copied[b]) cudaEventDestroy(S.copied[b]);
     }
+    if (S.st2) cudaStreamSynchronize(S.st2);
+    if (S.ev_fork) cudaEventDestroy(S.ev_fork);
+    if (S.ev_join) cudaEventDestroy(S.ev_join);
+    if (S.st2) cudaStreamDestroy(S.st2);
     if (S.st) cudaStreamDestroy(S.st);
     delete h;
 }
