@@ -15,13 +15,16 @@
 //   barrier  (all stresses written before the next phase A reads them)
 // plus, in the adjoint, every sfe steps either a store of the adjoint state
 // of the CTA's cells for the kernel accumulation after the pass
-// (k_snap_interaction), or the accumulation itself (one more barrier; the
-// shot's kernels stay in shared memory for the whole pass when the CTA has
-// room, and the checkpoint can be staged there during phase B). A thread
-// that updates one of the CTA's edge columns also writes
-// the new value into the neighbouring CTA's ghost column (st.shared::cluster,
-// made visible by the cluster barrier's release/acquire), so the stencils
-// only ever read the CTA's own shared memory. The x-differences walk the
+// (k_snap_interaction), or the accumulation itself (one cluster barrier
+// more; the shot's kernels stay in shared memory for the whole pass when
+// the CTA has room, and the checkpoint can be staged there during phase B).
+// A thread that updates one of the CTA's edge columns also writes the new
+// value into the neighbouring CTA's ghost column, with an asynchronous
+// store that completes on that CTA's mbarrier of the phase, so the stencils
+// only ever read the CTA's own shared memory. The barriers between the
+// phases are CTA barriers, followed, in the threads that read ghost columns,
+// by a wait on the phase's mbarrier: neighbours synchronise point to point,
+// without a cluster-wide barrier per step. The x-differences walk the
 // thread's columns with a sliding window: one new shared-memory load per
 // field per cell.
 //
@@ -91,9 +94,36 @@ __device__ __forceinline__ uint32_t cl_mapa(uint32_t addr, uint32_t rank) {
     asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
     return r;
 }
-__device__ __forceinline__ void cl_st(uint32_t addr, float v) {
-    asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(addr), "f"(v) : "memory");
+// Ghost pushes: an asynchronous store into a neighbour's shared memory that
+// completes `bytes` on that CTA's mbarrier (cluster addresses).
+__device__ __forceinline__ void cl_push(uint32_t addr, float v, uint32_t bar) {
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b32 [%0], %1, [%2];" ::"r"(addr),
+                 "r"(__float_as_uint(v)), "r"(bar)
+                 : "memory");
 }
+__device__ __forceinline__ void cl_mbar_init(uint32_t bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void cl_mbar_expect(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+// Waits (acquire, cluster scope) for phase `parity` of the mbarrier, at most
+// kClusterWaitIters tries; false when they ran out.
+constexpr int kClusterWaitIters = 1 << 20;
+__device__ __forceinline__ bool cl_mbar_wait(uint32_t bar, uint32_t parity) {
+    for (int i = 0; i < kClusterWaitIters; i++) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, "
+            "p;\n}"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+__device__ int g_cluster_wait_error;  // set when a ghost-column wait ran out of iterations
 
 // 4-byte asynchronous copy global -> shared (completed by cp_async_wait_all)
 __device__ __forceinline__ void cp_async4(float *dst, const float *src) {
@@ -169,9 +199,20 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
     constexpr int NKA = PSV ? 3 : 2;
     float *kacc = ckst + (g.stage ? (size_t)NV * (2 * cp + 3) * nz : 0);
     __shared__ int s_count;
+    // ghost columns of phase A (velocity; displacement too for an in-pass
+    // accumulation) and of phase B (stresses) landed from the neighbours
+    __shared__ __align__(8) unsigned long long s_gbar[2];
+    __shared__ int s_cdead;  // a ghost wait ran out: no mbarrier operation after it
+    const uint32_t gbar = (uint32_t)__cvta_generic_to_shared(s_gbar);
     int *map = reinterpret_cast<int *>(sm);
     for (int e = t; e < cp * nz; e += blockDim.x) map[e] = -1;
-    if (t == 0) s_count = 0;
+    if (t == 0) {
+        s_count = 0;
+        s_cdead = 0;
+        cl_mbar_init(gbar);
+        cl_mbar_init(gbar + 8u);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
     __syncthreads();
     for (int r = t; r < S.npts; r += blockDim.x) {
         const int i = S.pts_i[r] - x0, jj = S.pts_j[r];
@@ -237,6 +278,37 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
     // the thread owning columns 0, 1 sends them left; the one owning columns
     // cp-2, cp-1 sends them right (a CTA with a right neighbour holds cp columns)
     const bool edge_l = rank > 0 && grp == 0, edge_r = rank < R - 1 && cb + QM == cp;
+    // Ghost exchange. The edge threads push their new values into the
+    // neighbours' ghost columns with asynchronous stores that complete bytes
+    // on the receiving CTA's mbarrier of the phase (s_gbar[0]: phase A,
+    // s_gbar[1]: phase B); thread 0 arms it with the bytes this CTA receives
+    // (left neighbour's last column / right neighbour's first two in phase A,
+    // the left's last two / the right's first in phase B), and after the
+    // phase's CTA barrier the threads that read ghost columns (the edge
+    // groups) wait for it. No cluster-wide barrier per step: a neighbour can
+    // overwrite a ghost column only after it received this CTA's pushes of
+    // the phase that follows the reads of that column, and a thread pushes
+    // a column only after reading its own ghosts for it. (A cluster barrier
+    // with a cluster-scope release by every thread cost about a tenth of the
+    // step: the release waits for the thread's outstanding global stores.)
+    // the neighbours' mbarriers (formed where an edge thread pushes: held
+    // through the loop they would take registers from every thread)
+    auto gbar_l = [&]() { return cl_mapa(gbar, rank - 1); };
+    auto gbar_r = [&]() { return cl_mapa(gbar, rank + 1); };
+    auto ghost_expect = [&](int b) {
+        if (t == 0 && !*(volatile int *)&s_cdead) {
+            const uint32_t has_l = rank > 0 ? 1u : 0u, has_r = rank < R - 1 ? 1u : 0u;
+            const uint32_t bytes = b ? 4u * NSF * (uint32_t)nz * (2u * has_l + has_r)
+                                     : 4u * NV * ((ADJ && !snap) ? 2u : 1u) * (uint32_t)nz * (has_l + 2u * has_r);
+            cl_mbar_expect(gbar + 8u * b, bytes);
+        }
+    };
+    auto ghost_wait = [&](bool reader, int b, int it) {
+        if (reader && !*(volatile int *)&s_cdead && !cl_mbar_wait(gbar + 8u * b, (uint32_t)(it & 1))) {
+            s_cdead = 1;
+            atomicOr(&g_cluster_wait_error, 1);
+        }
+    };
 
     // Steps are counted as it = blk * sfe + ph (sfe > 0), kept by increments
     // instead of an integer division per step. Checkpoint index written after
@@ -327,6 +399,7 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
         // share the row shift of the group beside them
         const int dl = (fl & 16u) ? -g.dshift * g.rs : 0, dr = (fl & 32u) ? g.dshift * g.rs : 0;
         if (spm) cp_async_wait_all();  // this step's injection
+        ghost_expect(0);
         // ---- phase A: divergence, sources, velocity, displacement
         {
             float wa[NWA][4];  // x-window: columns c-2, c-1, c, c+1
@@ -394,16 +467,16 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
                     const uint32_t a = lf + 4u * (uint32_t)(cp + q + 2);
 #pragma unroll
                     for (int f = 0; f < NV; f++) {
-                        cl_st(a + 4u * (uint32_t)((FV + f) * fs), vn[f]);
-                        if (ADJ && (fl & 128u)) cl_st(a + 4u * (uint32_t)((FU + f) * fs), un[f]);
+                        cl_push(a + 4u * (uint32_t)((FV + f) * fs), vn[f], gbar_l());
+                        if (ADJ && (fl & 128u)) cl_push(a + 4u * (uint32_t)((FU + f) * fs), un[f], gbar_l());
                     }
                 }
                 if (q == QM - 1 && eR) {
                     const uint32_t a = rt + 4u;
 #pragma unroll
                     for (int f = 0; f < NV; f++) {
-                        cl_st(a + 4u * (uint32_t)((FV + f) * fs), vn[f]);
-                        if (ADJ && (fl & 128u)) cl_st(a + 4u * (uint32_t)((FU + f) * fs), un[f]);
+                        cl_push(a + 4u * (uint32_t)((FV + f) * fs), vn[f], gbar_r());
+                        if (ADJ && (fl & 128u)) cl_push(a + 4u * (uint32_t)((FU + f) * fs), un[f], gbar_r());
                     }
                 }
 #pragma unroll
@@ -414,7 +487,8 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
                 }
             }
         }
-        cl.sync();
+        __syncthreads();
+        ghost_wait(eL || eR, 0, it);
         // Global traffic of the step, issued here so that phase B's work hides
         // its latency before the next barrier: recorded samples, checkpoints
         // of velocity (after this step's update) and displacement (before the
@@ -445,6 +519,7 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
         }
         prefetch(it + 1);
         if (ADJ && g.stage && S.ckpt && S.sfe > 0 && ph == 0 && blk < S.nsfe) stage_ckpt(blk);
+        ghost_expect(1);
         // ---- phase B: velocity gradients and stress update
         {
             float wb[NV][4];  // x-window: columns c-1, c, c+1, c+2
@@ -483,12 +558,12 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
                 if (q == 0 && eL) {
                     const uint32_t a = lf + 4u * (uint32_t)(cp + 2);
 #pragma unroll
-                    for (int f = 0; f < NSF; f++) cl_st(a + 4u * (uint32_t)((FS + f) * fs), sv[f]);
+                    for (int f = 0; f < NSF; f++) cl_push(a + 4u * (uint32_t)((FS + f) * fs), sv[f], gbar_l() + 8u);
                 }
                 if (q >= QM - 2 && eR) {
                     const uint32_t a = rt + 4u * (uint32_t)(q - QM + 2);
 #pragma unroll
-                    for (int f = 0; f < NSF; f++) cl_st(a + 4u * (uint32_t)((FS + f) * fs), sv[f]);
+                    for (int f = 0; f < NSF; f++) cl_push(a + 4u * (uint32_t)((FS + f) * fs), sv[f], gbar_r() + 8u);
                 }
 #pragma unroll
                 for (int f = 0; f < NV; f++) {
@@ -499,7 +574,8 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
             }
         }
         if (ADJ) cp_async_wait_all();  // this thread's copies of the next step's adjoint sources
-        cl.sync();
+        __syncthreads();
+        ghost_wait(eL || eR, 1, it);
         // ---- adjoint with snap: the adjoint state of the owned grid cells at
         // each accumulation step, [slot][step][u fields, v fields][cell], for
         // the kernel accumulation after the pass (k_snap_interaction). Own
@@ -649,6 +725,9 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
             blk++;
         }
     }
+    // every push into this CTA has landed (the waits above); the barrier
+    // keeps each CTA's shared memory until the whole cluster is done
+    cl.sync();
     // the shared accumulators (written by this thread only) go to the shot's buffer
     if (ADJ && g.kacc) {
         const size_t kc = (size_t)i0 * nz + j;
@@ -799,6 +878,19 @@ static cudaLaunchConfig_t cluster_config(ClusterGeom g, int nz, int nslots, size
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     return cfg;
+}
+
+int cluster_wait_error() {
+    int e = 0;
+    if (cudaMemcpyFromSymbol(&e, g_cluster_wait_error, sizeof(int)) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return 1;
+    }
+    if (e) {
+        const int z = 0;
+        (void)cudaMemcpyToSymbol(g_cluster_wait_error, &z, sizeof(int));
+    }
+    return e;
 }
 
 cudaError_t launch_cluster(bool psv, bool adj, const Slot *d_slots, int nslots, ClusterGeom g, int nz, float *kpart,

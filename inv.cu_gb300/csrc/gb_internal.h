@@ -177,6 +177,9 @@ int cluster_max_threads(bool psv, int qmax);
 int cluster_occupancy(bool psv, ClusterGeom g, int nz);
 cudaError_t launch_cluster(bool psv, bool adj, const Slot *d_slots, int nslots, ClusterGeom g, int nz, float *kpart,
                            float *snap, cudaStream_t st);
+// returns (and clears) the device flag a ghost-column wait of the cluster
+// kernel that ran out of iterations sets
+int cluster_wait_error();
 // the kernel accumulation of a cluster adjoint pass that stored its adjoint
 // state (snap) instead of accumulating in the pass
 cudaError_t launch_snap_interaction(bool psv, const Slot *d_slots, int nslots, const float *snap, ClusterGeom g,

@@ -1109,6 +1109,10 @@ int Solver::run_cluster_pass(int kind, int n) {
     }
     GB_CUDA_TRY(cudaEventRecord(ev_pass1, st));
     GB_CUDA_TRY(cudaStreamSynchronize(st));
+    if (cluster_wait_error()) {
+        set_error("cluster pass: a ghost-column wait ran out of iterations; the pass is invalid");
+        return GB_ERR_CUDA;
+    }
     float ms = 0;
     GB_CUDA_TRY(cudaEventElapsedTime(&ms, ev_pass0, ev_pass1));
     if (adjp)
@@ -1125,6 +1129,11 @@ int Solver::run_cluster_pass(int kind, int n) {
 int Solver::book_forward_pass() {
     if (!fpass_pending) return GB_OK;
     GB_CUDA_TRY(cudaEventSynchronize(ev_fpass1));
+    if (cluster_wait_error()) {
+        fpass_pending = false;
+        set_error("cluster pass: a ghost-column wait ran out of iterations; the pass is invalid");
+        return GB_ERR_CUDA;
+    }
     float ms = 0;
     GB_CUDA_TRY(cudaEventElapsedTime(&ms, ev_fpass0, ev_fpass1));
     stats.forward_ms += ms;
