@@ -729,8 +729,9 @@ def run_c5(args):
     checkpoints. With --iterations N: the full inversion's setting (--shots,
     default 128; L-BFGS with memory 10; smoothing sigma 10 cells; lambda and
     mu inverted; initial model the true one smoothed by a Gaussian of 500 m)
-    for N iterations, once with BF16 checkpoints and once with FP32 ones,
-    reporting the time per iteration, the misfit history and the difference
+    for N iterations, with BF16 and with FP32 checkpoints (--precisions),
+    reporting the time per iteration, the misfit history, each final model's
+    error against the true model and, with both precisions, the difference
     between the two final models."""
     import __graft_entry__ as ge
 
@@ -789,7 +790,12 @@ def run_c5(args):
     sol.close()
     res = {}
     models = {}
+    names = [p.strip() for p in args.precisions.split(",") if p.strip()]
+    if not names or any(p not in ("bf16", "fp32") for p in names):
+        raise SystemExit("--precisions: bf16 and/or fp32")
     for prec, name in ((1, "bf16"), (0, "fp32")):
+        if name not in names:
+            continue
         cfg, sol = _solver_for(pkg, tmp, values, src, rec, nx, nz, h, init)
         sol.set_option("ckpt", prec)
         mis = pkg.Misfit.from_obs(0, sol, obs, pkg.GaussianFilter(nx, nz, 10))
@@ -811,20 +817,21 @@ def run_c5(args):
     def rel(a, b):
         return float(np.linalg.norm(a.astype(np.float64) - b) / np.linalg.norm(b.astype(np.float64)))
 
-    for name in ("bf16", "fp32"):
+    for name in names:
         res[name]["model_error_vs_true"] = {k: rel(models[name][k], true[q]) for q, k in enumerate(("lambda", "mu"))}
-    res["bf16_vs_fp32_model"] = {k: rel(models["bf16"][k], models["fp32"][k]) for k in ("lambda", "mu")}
-    res["bf16_vs_fp32_update"] = {
-        k: float(np.linalg.norm(models["bf16"][k].astype(np.float64) - models["fp32"][k]) /
-                 np.linalg.norm(models["fp32"][k].astype(np.float64) - init[q]))
-        for q, k in enumerate(("lambda", "mu"))}
+    if len(names) == 2:
+        res["bf16_vs_fp32_model"] = {k: rel(models["bf16"][k], models["fp32"][k]) for k in ("lambda", "mu")}
+        res["bf16_vs_fp32_update"] = {
+            k: float(np.linalg.norm(models["bf16"][k].astype(np.float64) - models["fp32"][k]) /
+                     np.linalg.norm(models["fp32"][k].astype(np.float64) - init[q]))
+            for q, k in enumerate(("lambda", "mu"))}
     res["initial_model_error_vs_true"] = {k: rel(init[q], true[q]) for q, k in enumerate(("lambda", "mu"))}
     _line("full inversion, s per L-BFGS iteration (P-SV 4096x1024, %d shots)" % nshot,
-          res["bf16"]["s_per_iteration"], "s/iteration",
-          {"workload": desc + ", L-BFGS memory 10, %d of 20 iterations, BF16 vs FP32 checkpoints, initial "
-                       "model smoothed by a 500 m Gaussian" % args.iterations},
+          res[names[0]]["s_per_iteration"], "s/iteration",
+          {"workload": desc + ", L-BFGS memory 10, %d of 20 iterations, %s checkpoints, initial "
+                       "model smoothed by a 500 m Gaussian" % (args.iterations, " and ".join(n.upper() for n in names))},
           higher_is_better=False, inversion=res,
-          projected_20_iterations_s=round(20 * res["bf16"]["s_per_iteration"], 0))
+          projected_20_iterations_s=round(20 * res[names[0]]["s_per_iteration"], 0))
 
 
 def run_profile_case(args):
@@ -971,6 +978,7 @@ def main():
     ap.add_argument("--shots", type=int, default=0,
                     help="shot count for c3/c5 (default 64; c5 16, or 128 with --iterations)")
     ap.add_argument("--iterations", type=int, default=0, help="c5: run that many L-BFGS iterations of the inversion")
+    ap.add_argument("--precisions", default="bf16,fp32", help="c5 inversion: checkpoint precisions to run")
     ap.add_argument("--requests", type=int, default=512, help="c4 request count")
     ap.add_argument("--rate", type=float, default=0.0,
                     help="c4 Poisson arrival rate (requests/s); 0: --load x the measured capacity")
