@@ -423,11 +423,18 @@ __device__ __forceinline__ CkGroup ckpt_group(const Slot &S, bool psv, int which
 // Field f of group g at cell k, in FP32: a copy, or the forward-staggered
 // differences of the kernel accumulation (the guards and arithmetic of
 // k_interaction's FP32 path: 0 where the reference skips a difference).
-// The state address of reference-layout cell k (i*nz + j) at the slot's pitch.
-__device__ __forceinline__ size_t state_addr(const Slot &S, size_t k) {
-    if (S.pz == S.nz) return k;
-    const size_t i = k / S.nz;
-    return i * S.pz + (k - i * S.nz);
+// Column i = k / nz and row j of reference-layout cell k among n cells: a
+// 32-bit division below 2^31 cells (the 64-bit one takes several times the
+// instructions, and these kernels divide once per cell).
+__device__ __forceinline__ void cell_ij(size_t k, int nz, size_t n, int &i, int &j) {
+    if (n < ((size_t)1 << 31)) {
+        const unsigned u = (unsigned)k, q = u / (unsigned)nz;
+        i = (int)q;
+        j = (int)(u - q * (unsigned)nz);
+    } else {
+        i = (int)(k / nz);
+        j = (int)(k - (size_t)i * nz);
+    }
 }
 
 // Every field of group g at cell k, in FP32: copies, or the forward-staggered
@@ -435,14 +442,15 @@ __device__ __forceinline__ size_t state_addr(const Slot &S, size_t k) {
 // k_interaction's FP32 path: 0 where the reference skips a difference), each
 // neighbour loaded once for all the group's fields.
 __device__ __forceinline__ void ckpt_values(const Slot &S, const CkGroup &g, size_t k, float *out) {
-    const size_t a = state_addr(S, k);
+    const int nx = S.nx, nz = S.nz, pz = S.pz;
+    int i, j;
+    cell_ij(k, nz, (size_t)nx * nz, i, j);
+    const size_t a = (size_t)i * pz + j;  // the state address at the slot's pitch
     if (g.kind == 0) {
         out[0] = __ldg(g.a + a);
         if (g.nfld > 1) out[1] = __ldg(g.b + a);
         return;
     }
-    const int nx = S.nx, nz = S.nz, pz = S.pz;
-    const int i = (int)(k / nz), j = (int)(k - (size_t)i * nz);
     const bool gx = i >= 1 && i < nx - 2, gz = j >= 1 && j < nz - 2;
     auto ddx = [&](const float *w) {
         return gx ? dplus(__ldg(w + a + pz), __ldg(w + a), __ldg(w + a + 2 * pz), __ldg(w + a - pz), S.c9x, S.c24x)
@@ -519,13 +527,19 @@ __global__ void k_ckpt_store(const Slot *__restrict__ slots, int kstep, int whic
     const CkGroup g = ckpt_group(S, psv, which_u, par);
     const size_t n = (size_t)S.nx * S.nz;
     size_t off[3];
-    float sc[3] = {1.f, 1.f, 1.f};
 #pragma unroll
-    for (int f = 0; f < 3; f++) {
-        off[f] = ((size_t)isfe * S.nf + g.q[f < g.nfld ? f : 0]) * n;
-        if (f >= g.nfld) continue;
-        if (S.ckpt_prec != CKPT_F32) sc[f] = ckpt_scale(S.ckpt_amax[(size_t)isfe * S.nf + g.q[f]], S.ckpt_prec);
-    }
+    for (int f = 0; f < 3; f++) off[f] = ((size_t)isfe * S.nf + g.q[f < g.nfld ? f : 0]) * n;
+    // the fields' scales, formed once per block (a division and an exponent
+    // split each; on small grids a thread stores only a cell or two)
+    __shared__ float s_sc[3];
+    if ((int)threadIdx.x < g.nfld)
+        s_sc[threadIdx.x] = S.ckpt_prec != CKPT_F32
+                                ? ckpt_scale(S.ckpt_amax[(size_t)isfe * S.nf + g.q[threadIdx.x]], S.ckpt_prec)
+                                : 1.f;
+    __syncthreads();
+    float sc[3];
+#pragma unroll
+    for (int f = 0; f < 3; f++) sc[f] = f < g.nfld ? s_sc[f] : 1.f;
     for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
         float v[3];
         ckpt_values(S, g, k, v);
@@ -580,9 +594,15 @@ __global__ void k_interaction(const Slot *__restrict__ slots, const KernelGroup 
     const KernelGroup &G = groups[blockIdx.y];
     const int nx = G.nx, nz = G.nz;
     const size_t n = (size_t)nx * nz;
-    const size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    const int i = (int)(k / nz), j = (int)(k - (size_t)i * nz);
+    if ((size_t)blockIdx.x * blockDim.x >= n) return;  // the whole block is past this group's grid
+    // threads past the grid work on the last cell and store nothing, so that
+    // every thread reaches the block barriers below
+    const size_t k0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    const bool live = k0 < n;
+    const size_t k = live ? k0 : n - 1;
+    __shared__ float s_inv[5];
+    int i, j;
+    cell_ij(k, nz, n, i, j);
     const bool gx = i >= 1 && i < nx - 2, gz = j >= 1 && j < nz - 2;
     float kl = G.inv_lambda ? G.k_lambda[k] : 0.f;
     float km = G.inv_mu ? G.k_mu[k] : 0.f;
@@ -600,11 +620,17 @@ __global__ void k_interaction(const Slot *__restrict__ slots, const KernelGroup 
         const bool q16 = S.ckpt_prec != CKPT_F32;
         const int base = (PSV && S.sh[0] != nullptr) ? ckpt_nf_sh(S.ckpt_prec) : 0;
         const int nfs = PSV ? ckpt_nf_psv(S.ckpt_prec) : ckpt_nf_sh(S.ckpt_prec);
-        float inv[5];
-        for (int q = 0; q < nfs; q++) {
-            const float a = S.ckpt_amax ? S.ckpt_amax[(size_t)isfe * S.nf + base + q] : 0.f;
-            inv[q] = 1.f / ckpt_scale(a, S.ckpt_prec);
+        // the inverse scales of the slot's checkpoint fields, formed once per
+        // block (a division and an exponent split each); the slot conditions
+        // above are the same for every thread of the block
+        __syncthreads();  // every thread has read the previous slot's
+        if ((int)threadIdx.x < nfs) {
+            const float a = S.ckpt_amax ? S.ckpt_amax[(size_t)isfe * S.nf + base + threadIdx.x] : 0.f;
+            s_inv[threadIdx.x] = 1.f / ckpt_scale(a, S.ckpt_prec);
         }
+        __syncthreads();
+        float inv[5];
+        for (int q = 0; q < nfs; q++) inv[q] = s_inv[q];
         // the slot's state at its pitch; checkpoints and kernels in the reference layout
         const int pz = S.pz;
         const size_t a = (size_t)i * pz + j;
@@ -666,6 +692,7 @@ __global__ void k_interaction(const Slot *__restrict__ slots, const KernelGroup 
             if (G.inv_mu) km = st_kmu_sh(km, dvydx, fdx, dvydz, fdz, ndt);
         }
     }
+    if (!live) return;
     if (G.inv_lambda) G.k_lambda[k] = kl;
     if (G.inv_mu) G.k_mu[k] = km;
     if (G.inv_rho) G.k_rho[k] = kr;
