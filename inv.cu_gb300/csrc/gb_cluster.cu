@@ -744,68 +744,100 @@ __global__ void __launch_bounds__(cluster_threads_for(PSV, QM), 1)
 // checkpoints (solver/fdm.h:583-606): for each cell, the differences and the
 // accumulation helpers (gb_stencil.h) of the in-pass accumulation, over the
 // accumulation steps in step order, so the per-shot kernels are
-// bit-identical to it. One
-// thread per cell of one shot (blockIdx.y = slot); neighbour offsets are 0
-// where the reference skips the difference, so no read leaves the grid.
+// bit-identical to it. A thread owns one row of kSnapCols consecutive
+// columns of one shot (blockIdx.y = slot; consecutive threads take
+// consecutive rows, so every load is coalesced): per step it loads the
+// displacement of columns c0-1 .. c0+kSnapCols+1 once into an x-window (the
+// x-differences of all its cells) plus each cell's z-neighbours and
+// velocities, instead of four loads per x-difference. Where the reference
+// skips a difference the neighbour offsets are 0 and the window's columns
+// are clamped to the grid, so no read leaves it; such differences are masked.
+constexpr int kSnapCols = 4;
 template <bool PSV>
 __global__ void k_snap_interaction(const Slot *__restrict__ slots, const float *__restrict__ snap, ClusterGeom g,
                                    float *__restrict__ kpart) {
-    constexpr int NV = PSV ? 2 : 1;
+    constexpr int NV = PSV ? 2 : 1, C = kSnapCols;
     const int slot = blockIdx.y;
     const Slot &S = slots[slot];
     if (!S.active || !S.ckpt || S.sfe <= 0) return;
     const int nx = g.nx, nz = g.nz;
     const size_t ncell = (size_t)nx * nz;
-    const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= ncell) return;
-    const int i = (int)(k / nz), j = (int)(k % nz);
-    const bool gx = i >= 1 && i < nx - 2, zv = j >= 1 && j < nz - 2;
-    const long ox = gx ? nz : 0, oz = zv ? 1 : 0;
+    const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned strip = tid / (unsigned)nz, j = tid - strip * (unsigned)nz;
+    const int c0 = (int)strip * C;  // first column of this thread
+    if (c0 >= nx) return;
+    const int nc = min(C, nx - c0);
+    const bool zv = j >= 1 && (int)j < nz - 2;
+    const long oz = zv ? 1 : 0;
+    // window column w (0 .. C+2) is grid column c0 - 1 + w, clamped
+    long wcol[C + 3];
+#pragma unroll
+    for (int w = 0; w < C + 3; w++) wcol[w] = (long)min(max(c0 - 1 + w, 0), nx - 1) * nz + j;
     const float ndt = (float)S.sfe * g.dt, c9x = g.c9x, c24x = g.c24x, c9z = g.c9z, c24z = g.c24z;
     const int base_ck = (PSV && S.sh[0] != nullptr) ? 2 : 0;
     const int nacc = min(S.nsfe, (g.nt - 1) / S.sfe + 1);
-    float kl = 0.f, km = 0.f, kr = 0.f;
-#pragma unroll 2
+    float kl[C], km[C], kr[C];
+#pragma unroll
+    for (int c = 0; c < C; c++) kl[c] = km[c] = kr[c] = 0.f;
+#pragma unroll 1
     for (int a = 0; a < nacc; a++) {
-        const float *ua = snap + ((size_t)slot * S.nsfe + a) * (2 * NV) * ncell + k;
-        const float *uf = static_cast<const float *>(S.ckpt) + ((size_t)a * S.nf + base_ck) * ncell + k;
-        float ux[NV], uzz[NV], fx[NV], fz[NV], vf[NV], va[NV];
+        const float *ua = snap + ((size_t)slot * S.nsfe + a) * (2 * NV) * ncell;
+        const float *uf = static_cast<const float *>(S.ckpt) + ((size_t)a * S.nf + base_ck) * ncell;
+        float ux[NV][C], uzz[NV][C], fx[NV][C], fz[NV][C], vf[NV][C], va[NV][C];
 #pragma unroll
         for (int f = 0; f < NV; f++) {
-            // every load is issued (the offsets are 0 where a difference is
-            // masked), so that the step's loads are all in flight together
             const float *u0 = ua + (size_t)f * ncell, *w0 = uf + (size_t)f * ncell;
-            const float a0 = u0[0], axp = u0[ox], axp2 = u0[2 * ox], axm = u0[-ox];
-            const float azp = u0[oz], azp2 = u0[2 * oz], azm = u0[-oz];
-            const float b0 = __ldg(w0), bxp = __ldg(w0 + ox), bxp2 = __ldg(w0 + 2 * ox), bxm = __ldg(w0 - ox);
-            const float bzp = __ldg(w0 + oz), bzp2 = __ldg(w0 + 2 * oz), bzm = __ldg(w0 - oz);
-            ux[f] = gx ? st_dplus(axp, a0, axp2, axm, c9x, c24x) : 0.f;
-            uzz[f] = zv ? st_dplus(azp, a0, azp2, azm, c9z, c24z) : 0.f;
-            fx[f] = gx ? st_dplus(bxp, b0, bxp2, bxm, c9x, c24x) : 0.f;
-            fz[f] = zv ? st_dplus(bzp, b0, bzp2, bzm, c9z, c24z) : 0.f;
-            vf[f] = __ldg(uf + (size_t)(NV + f) * ncell);
-            va[f] = ua[(size_t)(NV + f) * ncell];
+            float wa_[C + 3], wf_[C + 3];
+#pragma unroll
+            for (int w = 0; w < C + 3; w++) {
+                wa_[w] = u0[wcol[w]];
+                wf_[w] = __ldg(w0 + wcol[w]);
+            }
+#pragma unroll
+            for (int c = 0; c < C; c++) {
+                const int i = c0 + c;
+                const bool gx = i >= 1 && i < nx - 2;
+                const long k = wcol[c + 1];  // this cell
+                // (a cell whose x-difference is masked may see clamped
+                // copies in the window: the value is discarded)
+                ux[f][c] = gx ? st_dplus(wa_[c + 2], wa_[c + 1], wa_[c + 3], wa_[c], c9x, c24x) : 0.f;
+                fx[f][c] = gx ? st_dplus(wf_[c + 2], wf_[c + 1], wf_[c + 3], wf_[c], c9x, c24x) : 0.f;
+                const float a0 = wa_[c + 1], b0 = wf_[c + 1];
+                uzz[f][c] = zv ? st_dplus(u0[k + oz], a0, u0[k + 2 * oz], u0[k - oz], c9z, c24z) : 0.f;
+                fz[f][c] = zv ? st_dplus(__ldg(w0 + k + oz), b0, __ldg(w0 + k + 2 * oz), __ldg(w0 + k - oz), c9z, c24z)
+                              : 0.f;
+                vf[f][c] = __ldg(uf + (size_t)(NV + f) * ncell + k);
+                va[f][c] = ua[(size_t)(NV + f) * ncell + k];
+            }
         }
-        if (PSV) {
-            const float dvxdx = ux[0], dvxdz = uzz[0], dvzdx = ux[NV - 1], dvzdz = uzz[NV - 1];
-            const float fxdx = fx[0], fxdz = fz[0], fzdx = fx[NV - 1], fzdz = fz[NV - 1];
-            kr = st_krho_psv(kr, vf[0], va[0], vf[NV - 1], va[NV - 1], ndt);
-            km = st_kmu_psv(km, dvxdx, dvxdz, dvzdx, dvzdz, fxdx, fxdz, fzdx, fzdz, ndt);
-            kl = st_klambda_psv(kl, dvxdx, dvzdz, fxdx, fzdz, ndt);
-        } else {
-            kr = st_krho_sh(kr, vf[0], va[0], ndt);
-            km = st_kmu_sh(km, ux[0], fx[0], uzz[0], fz[0], ndt);
+#pragma unroll
+        for (int c = 0; c < C; c++) {
+            if (PSV) {
+                const float dvxdx = ux[0][c], dvxdz = uzz[0][c], dvzdx = ux[NV - 1][c], dvzdz = uzz[NV - 1][c];
+                const float fxdx = fx[0][c], fxdz = fz[0][c], fzdx = fx[NV - 1][c], fzdz = fz[NV - 1][c];
+                kr[c] = st_krho_psv(kr[c], vf[0][c], va[0][c], vf[NV - 1][c], va[NV - 1][c], ndt);
+                km[c] = st_kmu_psv(km[c], dvxdx, dvxdz, dvzdx, dvzdz, fxdx, fxdz, fzdx, fzdz, ndt);
+                kl[c] = st_klambda_psv(kl[c], dvxdx, dvzdz, fxdx, fzdz, ndt);
+            } else {
+                kr[c] = st_krho_sh(kr[c], vf[0][c], va[0][c], ndt);
+                km[c] = st_kmu_sh(km[c], ux[0][c], fx[0][c], uzz[0][c], fz[0][c], ndt);
+            }
         }
     }
-    if (PSV) kpart[((size_t)slot * 3 + 0) * ncell + k] = kl;
-    kpart[((size_t)slot * 3 + 1) * ncell + k] = km;
-    kpart[((size_t)slot * 3 + 2) * ncell + k] = kr;
+#pragma unroll
+    for (int c = 0; c < C; c++) {
+        if (c >= nc) break;
+        const size_t k = (size_t)(c0 + c) * nz + j;
+        if (PSV) kpart[((size_t)slot * 3 + 0) * ncell + k] = kl[c];
+        kpart[((size_t)slot * 3 + 1) * ncell + k] = km[c];
+        kpart[((size_t)slot * 3 + 2) * ncell + k] = kr[c];
+    }
 }
 
 cudaError_t launch_snap_interaction(bool psv, const Slot *d_slots, int nslots, const float *snap, ClusterGeom g,
                                     float *kpart, cudaStream_t st) {
-    const size_t ncell = (size_t)g.nx * g.nz;
-    const dim3 grid((unsigned)((ncell + 255) / 256), nslots);
+    const size_t threads = (size_t)((g.nx + kSnapCols - 1) / kSnapCols) * g.nz;
+    const dim3 grid((unsigned)((threads + 255) / 256), nslots);
     if (psv)
         k_snap_interaction<true><<<grid, 256, 0, st>>>(d_slots, snap, g, kpart);
     else
