@@ -25,6 +25,8 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
+#include <algorithm>
+
 #include "gb_internal.h"
 #include "gb_stencil.h"
 
@@ -556,22 +558,27 @@ __global__ void k_ckpt_store(const Slot *__restrict__ slots, int kstep, int whic
     }
 }
 
-static int ckpt_blocks(int n) {
-    int b = (n + 255) / 256;
-    return b < 1 ? 1 : (b > 1216 ? 1216 : b);
+// Blocks per slot (or group) for the grid-stride cell loops: about 2432
+// blocks in all, so that batches of many small grids (serving) do not launch
+// tens of thousands of blocks that find no work, at least 8 per slot, and no
+// more than the slot's cells need.
+static int cell_blocks(size_t n, int nslots) {
+    const int need = (int)std::min<size_t>((n + 255) / 256, 1 << 20);
+    const int share = std::max(8, 2432 / std::max(nslots, 1));
+    return std::max(1, std::min(need, share));
 }
 
 cudaError_t launch_ckpt_amax(const Slot *d_slots, int nslots, int n, int k, int which_u, bool psv,
                              cudaStream_t st) {
     if (nslots <= 0) return cudaSuccess;
-    k_ckpt_amax<<<dim3(ckpt_blocks(n), nslots), 256, 0, st>>>(d_slots, k, which_u, psv);
+    k_ckpt_amax<<<dim3(cell_blocks((size_t)n, nslots), nslots), 256, 0, st>>>(d_slots, k, which_u, psv);
     return cudaGetLastError();
 }
 
 cudaError_t launch_ckpt_store(const Slot *d_slots, int nslots, int n, int k, int which_u, bool psv,
                               cudaStream_t st) {
     if (nslots <= 0) return cudaSuccess;
-    k_ckpt_store<<<dim3(ckpt_blocks(n), nslots), 256, 0, st>>>(d_slots, k, which_u, psv);
+    k_ckpt_store<<<dim3(cell_blocks((size_t)n, nslots), nslots), 256, 0, st>>>(d_slots, k, which_u, psv);
     return cudaGetLastError();
 }
 
@@ -594,114 +601,117 @@ __global__ void k_interaction(const Slot *__restrict__ slots, const KernelGroup 
     const KernelGroup &G = groups[blockIdx.y];
     const int nx = G.nx, nz = G.nz;
     const size_t n = (size_t)nx * nz;
-    if ((size_t)blockIdx.x * blockDim.x >= n) return;  // the whole block is past this group's grid
-    // threads past the grid work on the last cell and store nothing, so that
-    // every thread reaches the block barriers below
-    const size_t k0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    const bool live = k0 < n;
-    const size_t k = live ? k0 : n - 1;
     __shared__ float s_inv[5];
-    int i, j;
-    cell_ij(k, nz, n, i, j);
-    const bool gx = i >= 1 && i < nx - 2, gz = j >= 1 && j < nz - 2;
-    float kl = G.inv_lambda ? G.k_lambda[k] : 0.f;
-    float km = G.inv_mu ? G.k_mu[k] : 0.f;
-    float kr = G.inv_rho ? G.k_rho[k] : 0.f;
-    for (int s = G.first; s < G.first + G.count; s++) {
-        const Slot &S = slots[s];
-        if (!S.active || !S.ckpt || S.sfe <= 0) continue;
-        const int it = S.it_base + kstep;
-        if (it < 0 || it >= S.nt || it % S.sfe != 0) continue;
-        const int isfe = it / S.sfe;
-        if (isfe >= S.nsfe) continue;
-        const int par = (S.par0 + kstep + 1) & 1;  // velocity written by this step
-        const float ndt = (float)S.sfe * S.dt;
-        const float c9x = S.c9x, c24x = S.c24x, c9z = S.c9z, c24z = S.c24z;
-        const bool q16 = S.ckpt_prec != CKPT_F32;
-        const int base = (PSV && S.sh[0] != nullptr) ? ckpt_nf_sh(S.ckpt_prec) : 0;
-        const int nfs = PSV ? ckpt_nf_psv(S.ckpt_prec) : ckpt_nf_sh(S.ckpt_prec);
-        // the inverse scales of the slot's checkpoint fields, formed once per
-        // block (a division and an exponent split each); the slot conditions
-        // above are the same for every thread of the block
-        __syncthreads();  // every thread has read the previous slot's
-        if ((int)threadIdx.x < nfs) {
-            const float a = S.ckpt_amax ? S.ckpt_amax[(size_t)isfe * S.nf + base + threadIdx.x] : 0.f;
-            s_inv[threadIdx.x] = 1.f / ckpt_scale(a, S.ckpt_prec);
+    // the block's cells, blockDim.x at a time (the loop bound is the same for
+    // every thread; threads past the grid work on the last cell and store
+    // nothing, so that every thread reaches the block barriers below)
+    for (size_t kb = blockIdx.x * (size_t)blockDim.x; kb < n; kb += (size_t)gridDim.x * blockDim.x) {
+        const size_t k0 = kb + threadIdx.x;
+        const bool live = k0 < n;
+        const size_t k = live ? k0 : n - 1;
+        int i, j;
+        cell_ij(k, nz, n, i, j);
+        const bool gx = i >= 1 && i < nx - 2, gz = j >= 1 && j < nz - 2;
+        float kl = G.inv_lambda ? G.k_lambda[k] : 0.f;
+        float km = G.inv_mu ? G.k_mu[k] : 0.f;
+        float kr = G.inv_rho ? G.k_rho[k] : 0.f;
+        for (int s = G.first; s < G.first + G.count; s++) {
+            const Slot &S = slots[s];
+            if (!S.active || !S.ckpt || S.sfe <= 0) continue;
+            const int it = S.it_base + kstep;
+            if (it < 0 || it >= S.nt || it % S.sfe != 0) continue;
+            const int isfe = it / S.sfe;
+            if (isfe >= S.nsfe) continue;
+            const int par = (S.par0 + kstep + 1) & 1;  // velocity written by this step
+            const float ndt = (float)S.sfe * S.dt;
+            const float c9x = S.c9x, c24x = S.c24x, c9z = S.c9z, c24z = S.c24z;
+            const bool q16 = S.ckpt_prec != CKPT_F32;
+            const int base = (PSV && S.sh[0] != nullptr) ? ckpt_nf_sh(S.ckpt_prec) : 0;
+            const int nfs = PSV ? ckpt_nf_psv(S.ckpt_prec) : ckpt_nf_sh(S.ckpt_prec);
+            // the inverse scales of the slot's checkpoint fields, formed once per
+            // block (a division and an exponent split each); the slot conditions
+            // above are the same for every thread of the block
+            __syncthreads();  // every thread has read the previous slot's
+            if ((int)threadIdx.x < nfs) {
+                const float a = S.ckpt_amax ? S.ckpt_amax[(size_t)isfe * S.nf + base + threadIdx.x] : 0.f;
+                s_inv[threadIdx.x] = 1.f / ckpt_scale(a, S.ckpt_prec);
+            }
+            __syncthreads();
+            float inv[5];
+            for (int q = 0; q < nfs; q++) inv[q] = s_inv[q];
+            // the slot's state at its pitch; checkpoints and kernels in the reference layout
+            const int pz = S.pz;
+            const size_t a = (size_t)i * pz + j;
+            auto grad = [&](const float *w, float &ddx, float &ddz) {
+                ddx = gx ? dplus(__ldg(w + a + pz), __ldg(w + a), __ldg(w + a + 2 * pz), __ldg(w + a - pz), c9x, c24x) : 0.f;
+                ddz = gz ? dplus(__ldg(w + a + 1), __ldg(w + a), __ldg(w + a + 2), __ldg(w + a - 1), c9z, c24z) : 0.f;
+            };
+            auto grad_ck = [&](int q, float &ddx, float &ddz) {
+                const float iv = inv[q];
+                ddx = gx ? dplus(ck_load(S, isfe, base + q, k + nz, n, iv), ck_load(S, isfe, base + q, k, n, iv),
+                                 ck_load(S, isfe, base + q, k + 2 * nz, n, iv), ck_load(S, isfe, base + q, k - nz, n, iv),
+                                 c9x, c24x)
+                         : 0.f;
+                ddz = gz ? dplus(ck_load(S, isfe, base + q, k + 1, n, iv), ck_load(S, isfe, base + q, k, n, iv),
+                                 ck_load(S, isfe, base + q, k + 2, n, iv), ck_load(S, isfe, base + q, k - 1, n, iv),
+                                 c9z, c24z)
+                         : 0.f;
+            };
+            auto ck = [&](int q) { return ck_load(S, isfe, base + q, k, n, inv[q]); };
+            if (PSV) {
+                float dvxdx, dvxdz, dvzdx, dvzdz;
+                grad(S.psv[UX], dvxdx, dvxdz);
+                grad(S.psv[UZ], dvzdx, dvzdz);
+                // forward: FP32 displacement (differences taken here), or the
+                // stored strains: divergence, normal-strain difference, shear sum (16-bit)
+                float fxdx = 0.f, fxdz = 0.f, fzdx = 0.f, fzdz = 0.f, fdv = 0.f, fdd = 0.f, fsh = 0.f;
+                if (q16) {
+                    fdv = ck(0);
+                    fdd = ck(1);
+                    fsh = ck(2);
+                } else {
+                    grad_ck(0, fxdx, fxdz);
+                    grad_ck(1, fzdx, fzdz);
+                }
+                if (G.inv_rho) {
+                    const float vx_fw = ck(q16 ? 3 : 2);
+                    const float vz_fw = ck(q16 ? 4 : 3);
+                    kr = st_krho_psv(kr, vx_fw, __ldg(S.psv[VX0 + par] + a), vz_fw, __ldg(S.psv[VZ0 + par] + a), ndt);
+                }
+                if (G.inv_mu)
+                    km = q16 ? st_kmu_psv_strain(km, dvxdx, dvxdz, dvzdx, dvzdz, fdv, fdd, fsh, ndt)
+                             : st_kmu_psv(km, dvxdx, dvxdz, dvzdx, dvzdz, fxdx, fxdz, fzdx, fzdz, ndt);
+                if (G.inv_lambda)
+                    kl = q16 ? st_klambda_psv_strain(kl, dvxdx, dvzdz, fdv, ndt)
+                             : st_klambda_psv(kl, dvxdx, dvzdz, fxdx, fzdz, ndt);
+            } else {
+                float dvydx, dvydz, fdx, fdz;
+                grad(S.sh[UY], dvydx, dvydz);
+                if (q16) {
+                    fdx = ck(0);
+                    fdz = ck(1);
+                } else {
+                    grad_ck(0, fdx, fdz);
+                }
+                if (G.inv_rho) {
+                    const float vy_fw = ck(q16 ? 2 : 1);
+                    kr = st_krho_sh(kr, vy_fw, __ldg(S.sh[VY0 + par] + a), ndt);
+                }
+                if (G.inv_mu) km = st_kmu_sh(km, dvydx, fdx, dvydz, fdz, ndt);
+            }
         }
-        __syncthreads();
-        float inv[5];
-        for (int q = 0; q < nfs; q++) inv[q] = s_inv[q];
-        // the slot's state at its pitch; checkpoints and kernels in the reference layout
-        const int pz = S.pz;
-        const size_t a = (size_t)i * pz + j;
-        auto grad = [&](const float *w, float &ddx, float &ddz) {
-            ddx = gx ? dplus(__ldg(w + a + pz), __ldg(w + a), __ldg(w + a + 2 * pz), __ldg(w + a - pz), c9x, c24x) : 0.f;
-            ddz = gz ? dplus(__ldg(w + a + 1), __ldg(w + a), __ldg(w + a + 2), __ldg(w + a - 1), c9z, c24z) : 0.f;
-        };
-        auto grad_ck = [&](int q, float &ddx, float &ddz) {
-            const float iv = inv[q];
-            ddx = gx ? dplus(ck_load(S, isfe, base + q, k + nz, n, iv), ck_load(S, isfe, base + q, k, n, iv),
-                             ck_load(S, isfe, base + q, k + 2 * nz, n, iv), ck_load(S, isfe, base + q, k - nz, n, iv),
-                             c9x, c24x)
-                     : 0.f;
-            ddz = gz ? dplus(ck_load(S, isfe, base + q, k + 1, n, iv), ck_load(S, isfe, base + q, k, n, iv),
-                             ck_load(S, isfe, base + q, k + 2, n, iv), ck_load(S, isfe, base + q, k - 1, n, iv),
-                             c9z, c24z)
-                     : 0.f;
-        };
-        auto ck = [&](int q) { return ck_load(S, isfe, base + q, k, n, inv[q]); };
-        if (PSV) {
-            float dvxdx, dvxdz, dvzdx, dvzdz;
-            grad(S.psv[UX], dvxdx, dvxdz);
-            grad(S.psv[UZ], dvzdx, dvzdz);
-            // forward: FP32 displacement (differences taken here), or the
-            // stored strains: divergence, normal-strain difference, shear sum (16-bit)
-            float fxdx = 0.f, fxdz = 0.f, fzdx = 0.f, fzdz = 0.f, fdv = 0.f, fdd = 0.f, fsh = 0.f;
-            if (q16) {
-                fdv = ck(0);
-                fdd = ck(1);
-                fsh = ck(2);
-            } else {
-                grad_ck(0, fxdx, fxdz);
-                grad_ck(1, fzdx, fzdz);
-            }
-            if (G.inv_rho) {
-                const float vx_fw = ck(q16 ? 3 : 2);
-                const float vz_fw = ck(q16 ? 4 : 3);
-                kr = st_krho_psv(kr, vx_fw, __ldg(S.psv[VX0 + par] + a), vz_fw, __ldg(S.psv[VZ0 + par] + a), ndt);
-            }
-            if (G.inv_mu)
-                km = q16 ? st_kmu_psv_strain(km, dvxdx, dvxdz, dvzdx, dvzdz, fdv, fdd, fsh, ndt)
-                         : st_kmu_psv(km, dvxdx, dvxdz, dvzdx, dvzdz, fxdx, fxdz, fzdx, fzdz, ndt);
-            if (G.inv_lambda)
-                kl = q16 ? st_klambda_psv_strain(kl, dvxdx, dvzdz, fdv, ndt)
-                         : st_klambda_psv(kl, dvxdx, dvzdz, fxdx, fzdz, ndt);
-        } else {
-            float dvydx, dvydz, fdx, fdz;
-            grad(S.sh[UY], dvydx, dvydz);
-            if (q16) {
-                fdx = ck(0);
-                fdz = ck(1);
-            } else {
-                grad_ck(0, fdx, fdz);
-            }
-            if (G.inv_rho) {
-                const float vy_fw = ck(q16 ? 2 : 1);
-                kr = st_krho_sh(kr, vy_fw, __ldg(S.sh[VY0 + par] + a), ndt);
-            }
-            if (G.inv_mu) km = st_kmu_sh(km, dvydx, fdx, dvydz, fdz, ndt);
+        if (live) {
+            if (G.inv_lambda) G.k_lambda[k] = kl;
+            if (G.inv_mu) G.k_mu[k] = km;
+            if (G.inv_rho) G.k_rho[k] = kr;
         }
     }
-    if (!live) return;
-    if (G.inv_lambda) G.k_lambda[k] = kl;
-    if (G.inv_mu) G.k_mu[k] = km;
-    if (G.inv_rho) G.k_rho[k] = kr;
 }
 
 cudaError_t launch_interaction(bool psv, const Slot *d_slots, const KernelGroup *d_groups, int ngroups,
                                int max_cells, int k, cudaStream_t st) {
     if (ngroups <= 0) return cudaSuccess;
-    dim3 grid((max_cells + 255) / 256, ngroups);
+    const dim3 grid(cell_blocks((size_t)max_cells, ngroups), ngroups);
     if (psv)
         k_interaction<true><<<grid, 256, 0, st>>>(d_slots, d_groups, k);
     else
