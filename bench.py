@@ -649,6 +649,8 @@ def run_c4(args):
             srv.set_option("tile", tile)
         if args.server_streams:
             srv.set_option("streams", args.server_streams)
+        if args.server_compact >= 0:
+            srv.set_option("compact", args.server_compact)
         for q, r in enumerate(reqs[:len(arrivals)]):
             srv.submit(arrival=float(arrivals[q]), **r)
         srv.run()
@@ -992,6 +994,9 @@ def main():
                     help="c4 step kernel configuration (0: the engine's default)")
     ap.add_argument("--server-streams", type=int, default=0,
                     help="c4 engine streams, 1 or 2 (0: the engine's default)")
+    ap.add_argument("--server-compact", type=int, default=-1,
+                    help="c4: 1 launches the requests' own tiles through a block map, 0 the largest request's "
+                         "tile count for every request (default: the engine's choice)")
     ap.add_argument("--profile-case", default="", help="run one small case for an ncu capture")
     ap.add_argument("--tile", type=int, default=3, help="kernel configuration for --profile-case")
     ap.add_argument("--tma", type=int, default=1, help="--profile-case: marching kernel bulk loads (1) or cp.async (0)")

@@ -329,7 +329,11 @@ gb_server *gb_server_create(int sfe, int ckpt_precision, double hbm_budget_gb, i
  * request's arrays stored at a pitch of nz rounded up to a multiple of 4,
  * default; 0: per-row cp.async; the results are the same), "streams" (2: the
  * SH requests' steps of a round run on a second stream beside the P-SV
- * ones, default; 1: one stream; the results are the same). */
+ * ones, default; 1: one stream; the results are the same), "compact" (1: a
+ * marching launch runs exactly the tiles of its requests, through a block
+ * map built each round, default; 0: as many blocks per request as the
+ * largest request has tiles, the surplus exiting at once; the results are
+ * the same). */
 int gb_server_set_option(gb_server *srv, const char *key, double value);
 /* Queues a request; returns its id (>= 0) or -1. */
 long long gb_server_submit(gb_server *srv, const gb_request_desc *req);

@@ -150,14 +150,18 @@ inline int csr_words(int ntiles, int nent, int ntr) { return 3 + ntiles + 1 + ne
 // ---------------------------------------------------------------- launchers
 // All launchers enqueue on `st` and return cudaGetLastError().
 // k is the launch's step index (see Slot::it_base).
+// block_map (marching kernel only; null: none): one entry per block,
+// (slot << 16) | tile, so a launch over slots of different sizes runs
+// exactly their tiles instead of max_tiles blocks for every slot; nmap is
+// the entry count (the grid), max_tiles is then unused.
 cudaError_t launch_step(bool psv, TileCfg tc, const Slot *d_slots, int nslots, int max_tiles, int k, bool tma,
-                        cudaStream_t st);
+                        cudaStream_t st, const unsigned *block_map = nullptr, int nmap = 0);
 // Marching kernel launch; tma = bulk tensor loads through the slots' maps.
 // march_tma_error returns (and clears) the device flag a bulk-load wait that
 // ran out of iterations sets.
 int march_tma_error();
 cudaError_t launch_march(bool psv, bool tma, int threads, int chunk, const Slot *d_slots, int nslots, int max_tiles, int k,
-                         cudaStream_t st);
+                         cudaStream_t st, const unsigned *block_map = nullptr, int nmap = 0);
 // Checkpoint of displacement before step k (which_u = 1) or velocity after
 // it (which_u = 0), for every slot with ckpt_write whose step is a
 // checkpoint step ((it + 1) % sfe == 0).

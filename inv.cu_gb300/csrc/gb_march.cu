@@ -137,9 +137,9 @@ __host__ __device__ constexpr int march_smem_words(int threads) {
 // itself ptxas settled the SH form at 64-80 registers with spills, and the
 // 16-shot 4096 x 1024 steps ran fastest with these caps (higher ones leave
 // fewer blocks resident).
-template <bool PSV, bool TMA>
+template <bool PSV, bool TMA, bool MAP>
 __global__ void __maxnreg__(PSV ? 128 : 96) k_march(const Slot *__restrict__ slots, int kstep,
-                                                            int chunk) {
+                                                            int chunk, const unsigned *__restrict__ block_map) {
     using W = MarchWords<PSV>;
     constexpr int NS = W::NS, NV = W::NV;
     constexpr int NZS = PSV ? 2 : 1;  // stress components with a z-derivative (sxz, szz | szy)
@@ -159,15 +159,29 @@ __global__ void __maxnreg__(PSV ? 128 : 96) k_march(const Slot *__restrict__ slo
 
     // Blocks run shot-minor (block b: shot b % nslots, tile b / nslots): the
     // same strip of every shot runs close together, so the model columns,
-    // shared by the shots, are read from HBM once and from L2 after.
-    const unsigned blk = blockIdx.y * gridDim.x + blockIdx.x;
-    const Slot &S = slots[blk % gridDim.y];
+    // shared by the shots, are read from HBM once and from L2 after. With a
+    // block map (requests of different sizes, each with its own model) block
+    // b takes the slot and tile of entry b, so no block is launched for a
+    // tile a slot does not have.
+    // (a form of its own: a run-time choice between the two pushed the SH
+    // bulk-load form past its register cap)
+    unsigned sidx, tile_u;
+    if constexpr (MAP) {
+        const unsigned e = __ldg(block_map + blockIdx.x);
+        sidx = e >> 16;
+        tile_u = e & 0xffffu;
+    } else {
+        const unsigned blk = blockIdx.y * gridDim.x + blockIdx.x;
+        sidx = blk % gridDim.y;
+        tile_u = blk / gridDim.y;
+    }
+    const Slot &S = slots[sidx];
     if (!S.active) return;
     const int it = S.it_base + kstep;
     if (it < 0 || it >= S.nt) return;
     const int par = (S.par0 + kstep) & 1;
     const int nx = S.nx, nz = S.nz, nt = S.nt, pz = S.pz;  // pz: address pitch of the grid arrays
-    const int tile = (int)(blk / gridDim.y);
+    const int tile = (int)tile_u;
     if (tile >= S.tiles_z * S.tiles_x) return;
     const int strip = tile % S.tiles_z, ck = tile / S.tiles_z;
     const int t = threadIdx.x;
@@ -672,32 +686,39 @@ int march_tma_error() {
     return e;
 }
 
-template <bool PSV, bool TMA>
+template <bool PSV, bool TMA, bool MAP>
 static cudaError_t launch_march_t(dim3 grid, int threads, size_t smem, const Slot *d_slots, int k, int chunk,
-                                  cudaStream_t st) {
+                                  cudaStream_t st, const unsigned *block_map) {
     static bool attr_set = false;
     if (!attr_set) {
-        const cudaError_t e = cudaFuncSetAttribute(k_march<PSV, TMA>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        const cudaError_t e = cudaFuncSetAttribute(k_march<PSV, TMA, MAP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                    march_smem_words<PSV>(kMaxMarchThreads) * 4);
         if (e != cudaSuccess) return e;
         attr_set = true;
     }
-    k_march<PSV, TMA><<<grid, threads, smem, st>>>(d_slots, k, chunk);
+    k_march<PSV, TMA, MAP><<<grid, threads, smem, st>>>(d_slots, k, chunk, block_map);
     return cudaGetLastError();
 }
 
+template <bool PSV, bool TMA>
+static cudaError_t launch_march_m(dim3 grid, int threads, size_t smem, const Slot *d_slots, int k, int chunk,
+                                  cudaStream_t st, const unsigned *block_map) {
+    return block_map ? launch_march_t<PSV, TMA, true>(grid, threads, smem, d_slots, k, chunk, st, block_map)
+                     : launch_march_t<PSV, TMA, false>(grid, threads, smem, d_slots, k, chunk, st, nullptr);
+}
+
 cudaError_t launch_march(bool psv, bool tma, int threads, int chunk, const Slot *d_slots, int nslots, int max_tiles,
-                         int k, cudaStream_t st) {
-    if (nslots <= 0 || max_tiles <= 0) return cudaSuccess;
+                         int k, cudaStream_t st, const unsigned *block_map, int nmap) {
+    if (block_map ? nmap <= 0 : (nslots <= 0 || max_tiles <= 0)) return cudaSuccess;
     if (threads < 32 || threads > kMaxMarchThreads || threads % 32 || chunk < 1 || chunk + 3 > kAxStage)
         return cudaErrorInvalidValue;
-    const dim3 grid(max_tiles, nslots);
+    const dim3 grid = block_map ? dim3((unsigned)nmap, 1) : dim3(max_tiles, nslots);
     const size_t smem = (size_t)(psv ? march_smem_words<true>(threads) : march_smem_words<false>(threads)) * 4;
     if (psv)
-        return tma ? launch_march_t<true, true>(grid, threads, smem, d_slots, k, chunk, st)
-                   : launch_march_t<true, false>(grid, threads, smem, d_slots, k, chunk, st);
-    return tma ? launch_march_t<false, true>(grid, threads, smem, d_slots, k, chunk, st)
-               : launch_march_t<false, false>(grid, threads, smem, d_slots, k, chunk, st);
+        return tma ? launch_march_m<true, true>(grid, threads, smem, d_slots, k, chunk, st, block_map)
+                   : launch_march_m<true, false>(grid, threads, smem, d_slots, k, chunk, st, block_map);
+    return tma ? launch_march_m<false, true>(grid, threads, smem, d_slots, k, chunk, st, block_map)
+               : launch_march_m<false, false>(grid, threads, smem, d_slots, k, chunk, st, block_map);
 }
 
 }  // namespace gb

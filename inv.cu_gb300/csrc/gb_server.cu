@@ -106,6 +106,14 @@ struct Server {
     KernelGroup *d_grp = nullptr, *h_grp[kStage] = {};
     cudaEvent_t copied[kStage] = {};
     int tab_cap = 0;
+    // Block maps of the round's marching launches (option "compact", on by
+    // default): one entry per tile of every request, (slot << 16) | tile,
+    // P-SV entries first, staged like the tables. Without them a launch runs
+    // max_tiles blocks for every request and the blocks past a smaller
+    // request's tiles exit at once.
+    bool compact = true;
+    unsigned *d_map = nullptr, *h_map[kStage] = {};
+    size_t map_cap = 0;
     // statistics
     int max_active = 0;
     long long rounds = 0, launches = 0;
@@ -461,11 +469,45 @@ int round_once(Server &S, std::vector<Req *> &act) {
         g.nx = order[q]->d.nx;
         g.nz = order[q]->d.nz;
     }
+    const int base_psv = 0, n_psv = counts[1][0] + counts[1][1];
+    const int base_sh = n_psv, n_sh = counts[0][0] + counts[0][1];
+    // block maps: [P-SV tiles][SH tiles], slots numbered within their system
+    // (16 bits each for the slot and the tile; a round beyond that launches
+    // max_tiles blocks per request instead)
+    bool use_map = S.compact && S.tile.threads > 0 && n <= 65536;
+    size_t map_off[2] = {0, 0}, map_n[2] = {0, 0};  // [sh, psv]
+    size_t total = 0;
+    for (int q = 0; use_map && q < n; q++) {
+        const size_t t = (size_t)h_tab[q].tiles_z * h_tab[q].tiles_x;
+        use_map = t <= 65536;
+        total += t;
+    }
+    if (use_map) {
+        if (total > S.map_cap) {
+            GB_CUDA_TRY(cudaStreamSynchronize(S.st));  // every staged map has been consumed
+            cudaFree(S.d_map);
+            for (int r = 0; r < Server::kStage; r++) cudaFreeHost(S.h_map[r]);
+            S.map_cap = std::max(total, 2 * S.map_cap);
+            GB_CUDA_TRY(cudaMalloc(&S.d_map, sizeof(unsigned) * S.map_cap));
+            for (int r = 0; r < Server::kStage; r++)
+                GB_CUDA_TRY(cudaMallocHost(&S.h_map[r], sizeof(unsigned) * S.map_cap));
+        }
+        unsigned *hm = S.h_map[b];
+        size_t e = 0;
+        for (int w = 1; w >= 0; w--) {
+            const int base = w ? base_psv : base_sh, cnt = w ? n_psv : n_sh;
+            map_off[w] = e;
+            for (int q = 0; q < cnt; q++) {
+                const unsigned t = (unsigned)(h_tab[base + q].tiles_z * h_tab[base + q].tiles_x);
+                for (unsigned tile = 0; tile < t; tile++) hm[e++] = ((unsigned)q << 16) | tile;
+            }
+            map_n[w] = e - map_off[w];
+        }
+        if (e) GB_CUDA_TRY(cudaMemcpyAsync(S.d_map, hm, sizeof(unsigned) * e, cudaMemcpyHostToDevice, S.st));
+    }
     GB_CUDA_TRY(cudaMemcpyAsync(S.d_tab, h_tab, sizeof(Slot) * n, cudaMemcpyHostToDevice, S.st));
     GB_CUDA_TRY(cudaMemcpyAsync(S.d_grp, h_grp, sizeof(KernelGroup) * n, cudaMemcpyHostToDevice, S.st));
     GB_CUDA_TRY(cudaEventRecord(S.copied[b], S.st));
-    const int base_psv = 0, n_psv = counts[1][0] + counts[1][1];
-    const int base_sh = n_psv, n_sh = counts[0][0] + counts[0][1];
     const bool q16 = S.prec != CKPT_F32;
     // the SH chain on its own stream when both systems have requests
     const bool fork = S.streams > 1 && n_psv > 0 && n_sh > 0;
@@ -492,7 +534,11 @@ int round_once(Server &S, std::vector<Req *> &act) {
                 GB_CUDA_TRY(launch_ckpt_store(tab, cnt, (int)max_n_fwd[w], k, 1, w, sw));
                 S.launches += q16 ? 2 : 1;
             }
-            GB_CUDA_TRY(launch_step(w, S.tile, tab, cnt, max_tiles[w], k, S.use_tma(), sw));
+            if (use_map)
+                GB_CUDA_TRY(launch_step(w, S.tile, tab, cnt, max_tiles[w], k, S.use_tma(), sw, S.d_map + map_off[w],
+                                        (int)map_n[w]));
+            else
+                GB_CUDA_TRY(launch_step(w, S.tile, tab, cnt, max_tiles[w], k, S.use_tma(), sw));
             S.launches++;
             if (k == S.sfe - 1 && cnt > nadj) {
                 if (q16) GB_CUDA_TRY(launch_ckpt_amax(tab, cnt, (int)max_n_fwd[w], k, 0, w, sw));
@@ -554,6 +600,10 @@ int gb_server_set_option(gb_server *h, const char *key, double value) {
     }
     if (k == "tma") {
         h->s.opt_tma = value != 0;
+        return GB_OK;
+    }
+    if (k == "compact") {
+        h->s.compact = value != 0;
         return GB_OK;
     }
     if (k == "streams") {
@@ -739,9 +789,11 @@ void gb_server_destroy(gb_server *h) {
     }
     cudaFree(S.d_tab);
     cudaFree(S.d_grp);
+    cudaFree(S.d_map);
     for (int b = 0; b < Server::kStage; b++) {
         cudaFreeHost(S.h_tab[b]);
         cudaFreeHost(S.h_grp[b]);
+        cudaFreeHost(S.h_map[b]);
         if (S.copied[b]) cudaEventDestroy(S.copied[b]);
     }
     if (S.st2) cudaStreamSynchronize(S.st2);

@@ -364,9 +364,10 @@ static cudaError_t launch_step_t(TileCfg tc, const Slot *d_slots, int nslots, in
 }
 
 cudaError_t launch_step(bool psv, TileCfg tc, const Slot *d_slots, int nslots, int max_tiles, int k, bool tma,
-                        cudaStream_t st) {
+                        cudaStream_t st, const unsigned *block_map, int nmap) {
+    if (tc.threads) return launch_march(psv, tma, tc.threads, tc.tx, d_slots, nslots, max_tiles, k, st, block_map, nmap);
+    if (block_map) return cudaErrorInvalidValue;
     if (nslots <= 0 || max_tiles <= 0) return cudaSuccess;
-    if (tc.threads) return launch_march(psv, tma, tc.threads, tc.tx, d_slots, nslots, max_tiles, k, st);
     return psv ? launch_step_t<true>(tc, d_slots, nslots, max_tiles, k, st)
                : launch_step_t<false>(tc, d_slots, nslots, max_tiles, k, st);
 }
