@@ -67,9 +67,16 @@ struct Req {
     int nsfe = 0, nf = 0, ncomp = 0;
     int pz = 0;              // address pitch of the state and model arrays
     void *tmaps = nullptr;   // tensor maps of the fields (bulk loads), or null
+    // host data the admission's uploads read; kept until the request leaves,
+    // so the admission does not wait for its copies
+    std::vector<float> h_ax, h_az, h_stf;
+    std::vector<int> h_csr;
+    std::vector<char> h_maps;
+    std::vector<TraceRefS> h_refs;
     // progress
-    int phase = 0;  // 0 waiting, 1 forward, 2 adjoint, 3 done
+    int phase = 0;  // 0 waiting, 1 forward, 2 adjoint, 4 results being copied out, 3 done
     int it = 0;
+    int pin = -1;  // pinned result buffer while phase is 4
     double t_admit = 0, t_done = 0;
     double misfit = 0;
     std::vector<float> res[3];
@@ -114,6 +121,22 @@ struct Server {
     bool compact = true;
     unsigned *d_map = nullptr, *h_map[kStage] = {};
     size_t map_cap = 0;
+    // Pinned result buffers. A request that finishes its adjoint has its
+    // kernels and per-trace misfit values copied into one, behind the
+    // buffer's event, and frees its device block; it is finalised (results
+    // into its host vectors, misfit summed, completion time read from the
+    // event) once that event has completed. Admissions, phase changes and
+    // completions thus never wait for the stream, and the host prepares the
+    // next rounds while the GPU runs.
+    static constexpr int kPins = 8;
+    struct Pin {
+        char *buf = nullptr;
+        cudaEvent_t ev = nullptr;
+        Req *owner = nullptr;
+    };
+    Pin pins[kPins];
+    size_t pin_bytes = 0;
+    cudaEvent_t ev_t0 = nullptr;  // recorded when a run starts: the origin of the completion times
     // statistics
     int max_active = 0;
     long long rounds = 0, launches = 0;
@@ -274,7 +297,9 @@ int admit(Server &S, Req &r) {
 
     // host-side preparation
     const float xmax = d.dx * (d.nx - 1), zmax = d.dz * (d.nz - 1);
-    std::vector<float> hax(d.nx, 1.f), haz(d.nz, 1.f);
+    std::vector<float> &hax = r.h_ax, &haz = r.h_az;
+    hax.assign(d.nx, 1.f);
+    haz.assign(d.nz, 1.f);
     const int w = d.abs_width;
     const float a = d.abs_alpha;
     for (int i = 0; i < d.nx; i++) {
@@ -285,7 +310,8 @@ int admit(Server &S, Req &r) {
         if (d.abs_bottom && j > d.nz - w) haz[j] *= expf(-powf(a * (float)(w + j - d.nz), 2));
         if (d.abs_top && j + 1 < w) haz[j] *= expf(-powf(a * (float)(w - j - 1), 2));
     }
-    std::vector<float> hstf(3 * (size_t)d.nt);
+    std::vector<float> &hstf = r.h_stf;
+    hstf.assign(3 * (size_t)d.nt, 0.f);
     ricker1(d.nt, d.dt, d.src + 3, hstf.data(), hstf.data() + d.nt, hstf.data() + 2 * d.nt);
     const std::vector<int> si = {calc_idx(d.src[0], xmax, d.nx)}, sj = {calc_idx(d.src[1], zmax, d.nz)};
     std::vector<int> ri(d.nrec), rj(d.nrec);
@@ -296,7 +322,11 @@ int admit(Server &S, Req &r) {
     const std::vector<int> c1 = csr_for(S.tile, d.nx, d.nz, si, sj, true);
     const std::vector<int> c2 = csr_for(S.tile, d.nx, d.nz, ri, rj, true);
     const std::vector<int> c3 = csr_for(S.tile, d.nx, d.nz, ri, rj, false);
-    GB_CUDA_TRY(cudaMallocAsync((void **)&r.csr_src, (c1.size() + c2.size() + c3.size()) * 4, S.st));
+    r.h_csr.clear();
+    r.h_csr.insert(r.h_csr.end(), c1.begin(), c1.end());
+    r.h_csr.insert(r.h_csr.end(), c2.begin(), c2.end());
+    r.h_csr.insert(r.h_csr.end(), c3.begin(), c3.end());
+    GB_CUDA_TRY(cudaMallocAsync((void **)&r.csr_src, r.h_csr.size() * 4, S.st));
     r.csr_rin = r.csr_src + c1.size();
     r.csr_rec = r.csr_rin + c2.size();
 
@@ -314,7 +344,8 @@ int admit(Server &S, Req &r) {
     // tensor maps of the state and model fields for the marching kernel's
     // bulk loads, for its strips of S.tile.threads rows
     r.tmaps = nullptr;
-    std::vector<char> hmaps((size_t)TMAP_N * TMAP_BYTES);
+    std::vector<char> &hmaps = r.h_maps;
+    hmaps.assign((size_t)TMAP_N * TMAP_BYTES, 0);
     if (S.use_tma()) {
         const float *sh_state = d.psv ? nullptr : r.state, *psv_state = d.psv ? r.state : nullptr;
         if (encode_slot_maps(hmaps.data(), d.psv ? psv_state : sh_state, !d.psv, d.psv != 0, r.rinv, r.mu, r.lam,
@@ -328,9 +359,7 @@ int admit(Server &S, Req &r) {
     GB_CUDA_TRY(cudaMemcpyAsync(r.ax, hax.data(), d.nx * 4, cudaMemcpyHostToDevice, S.st));
     GB_CUDA_TRY(cudaMemcpyAsync(r.az, haz.data(), d.nz * 4, cudaMemcpyHostToDevice, S.st));
     GB_CUDA_TRY(cudaMemcpyAsync(r.stf, hstf.data(), hstf.size() * 4, cudaMemcpyHostToDevice, S.st));
-    GB_CUDA_TRY(cudaMemcpyAsync(r.csr_src, c1.data(), c1.size() * 4, cudaMemcpyHostToDevice, S.st));
-    GB_CUDA_TRY(cudaMemcpyAsync(r.csr_rin, c2.data(), c2.size() * 4, cudaMemcpyHostToDevice, S.st));
-    GB_CUDA_TRY(cudaMemcpyAsync(r.csr_rec, c3.data(), c3.size() * 4, cudaMemcpyHostToDevice, S.st));
+    GB_CUDA_TRY(cudaMemcpyAsync(r.csr_src, r.h_csr.data(), r.h_csr.size() * 4, cudaMemcpyHostToDevice, S.st));
     if (d.obs)
         GB_CUDA_TRY(cudaMemcpyAsync(obb, d.obs, (size_t)r.ncomp * tr * 4, cudaMemcpyHostToDevice, S.st));
     else
@@ -340,15 +369,15 @@ int admit(Server &S, Req &r) {
     GB_CUDA_TRY(cudaMemsetAsync(r.amax, 0, (size_t)r.nsfe * r.nf * 4, S.st));
     GB_CUDA_TRY(cudaMemsetAsync(outb, 0, (size_t)r.ncomp * tr * 4, S.st));
     GB_CUDA_TRY(launch_taper(r.tw, d.dt, d.nt, S.st));
-    std::vector<TraceRefS> refs((size_t)r.ncomp * d.nrec);
+    std::vector<TraceRefS> &refs = r.h_refs;
+    refs.resize((size_t)r.ncomp * d.nrec);
     for (int ir = 0; ir < d.nrec; ir++)
         for (int q = 0; q < r.ncomp; q++) {
             const size_t off = (size_t)ir * d.nt;
             refs[(size_t)ir * r.ncomp + q] = {outb + q * tr + off, obb + q * tr + off, adb + q * tr + off};
         }
     GB_CUDA_TRY(cudaMemcpyAsync(r.refs, refs.data(), refs.size() * sizeof(TraceRefS), cudaMemcpyHostToDevice, S.st));
-    // the host vectors above die at return: finish the copies now
-    GB_CUDA_TRY(cudaStreamSynchronize(S.st));
+    // no wait: the host data stays with the request until it leaves
     r.phase = 1;
     r.it = 0;
     S.used += r.bytes;
@@ -560,6 +589,89 @@ int round_once(Server &S, std::vector<Req *> &act) {
     return GB_OK;
 }
 
+size_t pin_need(const Req &r) {
+    return align256((size_t)3 * r.d.nx * r.d.nz * 4) + (size_t)r.ncomp * r.d.nrec * 8;
+}
+
+// Results of the request in pin p (its event has completed) into its host
+// vectors; its completion time is the event's time since the run began.
+int finalize(Server &S, int p, size_t &done) {
+    Server::Pin &P = S.pins[p];
+    Req &r = *P.owner;
+    const size_t n = (size_t)r.d.nx * r.d.nz;
+    const float *k = reinterpret_cast<const float *>(P.buf);
+    for (int q = 0; q < 3; q++) r.res[q].assign(k + q * n, k + (q + 1) * n);
+    const double *v = reinterpret_cast<const double *>(P.buf + align256(3 * n * 4));
+    r.misfit = 0;
+    for (int t = 0; t < r.ncomp * r.d.nrec; t++) r.misfit += v[t];
+    float ms = 0;
+    GB_CUDA_TRY(cudaEventElapsedTime(&ms, S.ev_t0, P.ev));
+    r.t_done = ms * 1e-3;
+    r.phase = 3;
+    r.pin = -1;
+    r.h_ax = {};
+    r.h_az = {};
+    r.h_stf = {};
+    r.h_csr = {};
+    r.h_maps = {};
+    r.h_refs = {};
+    P.owner = nullptr;
+    done++;
+    return GB_OK;
+}
+
+// Finalises every pinned result whose copies have completed (wait = true:
+// every one, waiting for them).
+int reap(Server &S, size_t &done, bool wait) {
+    for (int p = 0; p < Server::kPins; p++) {
+        if (!S.pins[p].owner) continue;
+        if (wait) {
+            GB_CUDA_TRY(cudaEventSynchronize(S.pins[p].ev));
+        } else {
+            const cudaError_t q = cudaEventQuery(S.pins[p].ev);
+            if (q == cudaErrorNotReady) {
+                if (cudaPeekAtLastError() == cudaErrorNotReady) (void)cudaGetLastError();
+                continue;
+            }
+            GB_CUDA_TRY(q);
+        }
+        const int rc = finalize(S, p, done);
+        if (rc) return rc;
+    }
+    return GB_OK;
+}
+
+// Copies a finished request's kernels and misfit values into a free pinned
+// buffer (waiting for the oldest one if none is free) and frees its block.
+int retire(Server &S, Req &r, size_t &done) {
+    int p = -1;
+    for (int q = 0; q < Server::kPins && p < 0; q++)
+        if (!S.pins[q].owner) p = q;
+    if (p < 0) {
+        GB_CUDA_TRY(cudaEventSynchronize(S.pins[0].ev));
+        const int rc = finalize(S, 0, done);
+        if (rc) return rc;
+        p = 0;
+    }
+    Server::Pin &P = S.pins[p];
+    const size_t n = (size_t)r.d.nx * r.d.nz;
+    for (int q = 0; q < 3; q++)
+        GB_CUDA_TRY(cudaMemcpyAsync(P.buf + q * n * 4, r.k[q], n * 4, cudaMemcpyDeviceToHost, S.st));
+    const int ntr = r.ncomp * r.d.nrec;
+    if (ntr)
+        GB_CUDA_TRY(cudaMemcpyAsync(P.buf + align256(3 * n * 4), r.val, (size_t)ntr * 8, cudaMemcpyDeviceToHost, S.st));
+    GB_CUDA_TRY(cudaEventRecord(P.ev, S.st));
+    GB_CUDA_TRY(cudaFreeAsync(r.blk, S.st));
+    GB_CUDA_TRY(cudaFreeAsync(r.csr_src, S.st));
+    r.blk = nullptr;
+    r.csr_src = nullptr;
+    r.phase = 4;
+    r.pin = p;
+    P.owner = &r;
+    S.used -= r.bytes;  // stream-ordered: a later admission's allocation follows the free
+    return GB_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -660,8 +772,24 @@ int gb_server_run(gb_server *h) {
         S.reqs[q].phase = 0;
         S.reqs[q].blk = nullptr;
     }
+    // pinned result buffers for the largest request
+    size_t need = 0;
+    for (const Req &r : S.reqs) need = std::max(need, pin_need(r));
+    if (need > S.pin_bytes) {
+        GB_CUDA_TRY(cudaStreamSynchronize(S.st));
+        for (auto &P : S.pins) {
+            cudaFreeHost(P.buf);
+            P.buf = nullptr;
+        }
+        for (auto &P : S.pins) GB_CUDA_TRY(cudaMallocHost((void **)&P.buf, need));
+        S.pin_bytes = need;
+    }
+    for (auto &P : S.pins)
+        if (!P.ev) GB_CUDA_TRY(cudaEventCreate(&P.ev));
+    if (!S.ev_t0) GB_CUDA_TRY(cudaEventCreate(&S.ev_t0));
     std::vector<Req *> act;
     const auto t0 = std::chrono::steady_clock::now();
+    GB_CUDA_TRY(cudaEventRecord(S.ev_t0, S.st));
     size_t done = 0;
     while (done < S.reqs.size()) {
         // admission in arrival order, by HBM budget and free slots
@@ -677,6 +805,9 @@ int gb_server_run(gb_server *h) {
         }
         S.max_active = std::max(S.max_active, (int)act.size());
         if (act.empty()) {
+            // nothing on the GPU but results being copied out: wait for them
+            const int rc = reap(S, done, true);
+            if (rc) return rc;
             if (waiting.empty()) break;
             const double wait = S.reqs[waiting.front()].d.arrival - now_s(t0);
             if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(std::min(wait, 0.01)));
@@ -692,39 +823,29 @@ int gb_server_run(gb_server *h) {
                 continue;
             }
             const gb_request_desc &d = r->d;
-            const size_t n = (size_t)d.nx * d.nz;
             if (r->phase == 1) {
                 // waveform misfit and adjoint sources (misfit/waveform.h:4-40)
                 const int ntr = r->ncomp * d.nrec;
                 if (ntr) GB_CUDA_TRY(launch_waveform_refs(r->refs, r->tw, ntr, d.nt, std::sqrt(d.dt), r->val, S.st));
                 S.launches++;
-                std::vector<double> v(ntr);
-                if (ntr)
-                    GB_CUDA_TRY(cudaMemcpyAsync(v.data(), r->val, ntr * 8, cudaMemcpyDeviceToHost, S.st));
+                // (the per-trace values stay on the device until the
+                // request leaves; its misfit is their sum, formed then)
                 GB_CUDA_TRY(cudaMemsetAsync(r->state, 0, (size_t)(d.psv ? NPSV : NSH) * d.nx * r->pz * 4, S.st));
-                GB_CUDA_TRY(cudaStreamSynchronize(S.st));
-                r->misfit = 0;
-                for (double x : v) r->misfit += x;
                 r->phase = 2;
                 r->it = 0;
                 still.push_back(r);
             } else {
-                for (int q = 0; q < 3; q++) {
-                    r->res[q].resize(n);
-                    GB_CUDA_TRY(cudaMemcpyAsync(r->res[q].data(), r->k[q], n * 4, cudaMemcpyDeviceToHost, S.st));
-                }
-                GB_CUDA_TRY(cudaFreeAsync(r->blk, S.st));
-                GB_CUDA_TRY(cudaFreeAsync(r->csr_src, S.st));
-                GB_CUDA_TRY(cudaStreamSynchronize(S.st));
-                r->blk = nullptr;
-                r->csr_src = nullptr;
-                r->t_done = now_s(t0);
-                r->phase = 3;
-                S.used -= r->bytes;
-                done++;
+                const int rc2 = retire(S, *r, done);
+                if (rc2) return rc2;
             }
         }
         act.swap(still);
+        rc = reap(S, done, false);
+        if (rc) return rc;
+    }
+    {
+        const int rc = reap(S, done, true);
+        if (rc) return rc;
     }
     GB_CUDA_TRY(cudaStreamSynchronize(S.st));
     S.run_s = now_s(t0);
@@ -790,6 +911,11 @@ void gb_server_destroy(gb_server *h) {
     cudaFree(S.d_tab);
     cudaFree(S.d_grp);
     cudaFree(S.d_map);
+    for (auto &P : S.pins) {
+        cudaFreeHost(P.buf);
+        if (P.ev) cudaEventDestroy(P.ev);
+    }
+    if (S.ev_t0) cudaEventDestroy(S.ev_t0);
     for (int b = 0; b < Server::kStage; b++) {
         cudaFreeHost(S.h_tab[b]);
         cudaFreeHost(S.h_grp[b]);
