@@ -993,7 +993,7 @@ def main():
     ap.add_argument("--server-tile", type=int, default=0,
                     help="c4 step kernel configuration (0: the engine's default)")
     ap.add_argument("--server-streams", type=int, default=0,
-                    help="c4 engine streams, 1 or 2 (0: the engine's default)")
+                    help="c4 engine streams, 1, 2 or 4 (0: the engine's default)")
     ap.add_argument("--server-compact", type=int, default=-1,
                     help="c4: 1 launches the requests' own tiles through a block map, 0 the largest request's "
                          "tile count for every request (default: the engine's choice)")

@@ -327,9 +327,11 @@ gb_server *gb_server_create(int sfe, int ckpt_precision, double hbm_budget_gb, i
  * as gb_solver_set_option; default 9, marching strips of 120 rows), "tma"
  * (1: the marching kernel loads grid columns with bulk tensor copies, each
  * request's arrays stored at a pitch of nz rounded up to a multiple of 4,
- * default; 0: per-row cp.async; the results are the same), "streams" (2: the
- * SH requests' steps of a round run on a second stream beside the P-SV
- * ones, default; 1: one stream; the results are the same), "compact" (1: a
+ * default; 0: per-row cp.async; the results are the same), "streams" (4:
+ * each wave system's requests split into two groups, each group's steps of a
+ * round on its own stream, default; 2: the SH requests' steps on a second
+ * stream beside the P-SV ones; 1: one stream; the results are the same),
+ * "compact" (1: a
  * marching launch runs exactly the tiles of its requests, through a block
  * map built each round, default; 0: as many blocks per request as the
  * largest request has tiles, the surplus exiting at once; the results are
