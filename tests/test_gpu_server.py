@@ -93,15 +93,16 @@ def test_bulk_loads_and_pitch_identical_to_per_row_loads(gpu):
     multiple of 4 so that the marching kernel can load their columns with
     bulk tensor copies: the kernels and misfits are bit-identical to those
     of per-row cp.async loads (pitch unchanged there as well), to the 2-D
-    tile kernel's, which keeps the reference layout, to runs with the
-    SH and P-SV steps on one stream and with each system's requests split
-    over two streams, and to a run that launches the largest
+    tile kernel's, which keeps the reference layout, to runs with all
+    steps on one stream and with the SH steps on one stream beside the P-SV
+    ones (the default splits each system's requests over two streams), and
+    to a run that launches the largest
     request's tile count for every request instead of a block map of the
     requests' own tiles."""
     mix = MIX + [(1, 77, 61, 200, 7), (0, 95, 33, 200, 8)]
     reqs = [request(*m)[1] for m in mix]
     out = []
-    for opts in ({}, {"tma": 0}, {"tile": 3}, {"streams": 1}, {"streams": 4}, {"compact": 0}):
+    for opts in ({}, {"tma": 0}, {"tile": 3}, {"streams": 1}, {"streams": 2}, {"compact": 0}):
         srv = gpu.Server(sfe=10)
         for k, v in opts.items():
             srv.set_option(k, v)
