@@ -390,7 +390,9 @@ def run_ours(args, ws, rank, local):
         pkg.lib().gb_device_sync()
         t0 = time.perf_counter()
         pkg.check(pkg.lib().gb_set_model_grid(sol._h, *[pkg._ptr(m.array) for m in h_model]))
-        pkg.check(pkg.lib().gb_misfit_set_obs(mis._h, None, pkg._ptr(h_obs.array), None))
+        # the observed traces' upload overlaps the forward pass (the misfit
+        # stages wait for it); it completes inside mis.run
+        pkg.check(pkg.lib().gb_misfit_set_obs_async(mis._h, None, pkg._ptr(h_obs.array), None))
         mis_val = mis.run(kernel=True)
         for q, which in enumerate((pkg.GB_K_MU, pkg.GB_K_RHO)):
             pkg.check(pkg.lib().gb_memcpy_d2h(h_k[q].ptr, sol.ptr(which), cells * 4))

@@ -248,6 +248,13 @@ gb_misfit *gb_misfit_create_obs(int type, gb_solver *s, gb_filter *f, const floa
                                 const float *obs_z);
 /* Replaces the observed traces of every shot, host arrays as above. */
 int gb_misfit_set_obs(gb_misfit *m, const float *obs_x, const float *obs_y, const float *obs_z);
+/* The same copies, queued on an upload stream of the misfit's own: the call
+ * returns at once, and the next gb_misfit_run overlaps them with its forward
+ * pass (only its misfit stage waits for them). The host arrays must stay
+ * unchanged until that run returns; pinned memory (cudaMallocHost) makes the
+ * copies asynchronous. No counterpart in the reference, whose observed traces
+ * are read once at Misfit::init (misfit/misfit.h:91-151). */
+int gb_misfit_set_obs_async(gb_misfit *m, const float *obs_x, const float *obs_y, const float *obs_z);
 /* Misfit::run (misfit/misfit.h:15-51): all shots, batched; with kernel != 0
  * also the adjoint kernels, then the filter on k_lambda, k_mu, k_rho. */
 int gb_misfit_run(gb_misfit *m, int kernel, int snapshot, double *value);

@@ -120,6 +120,7 @@ def _declare(lib):
         "gb_misfit_create": (_vp, [_vp, _vp, _vp]),
         "gb_misfit_create_obs": (_vp, [ctypes.c_int, _vp, _vp, _fp, _fp, _fp]),
         "gb_misfit_set_obs": (ctypes.c_int, [_vp, _fp, _fp, _fp]),
+        "gb_misfit_set_obs_async": (ctypes.c_int, [_vp, _fp, _fp, _fp]),
         "gb_misfit_run": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
         "gb_misfit_trace_values": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double), ctypes.c_size_t]),
         "gb_misfit_destroy": (None, [_vp]),
@@ -494,9 +495,17 @@ class Misfit:
         arr = {c: (_f32(obs[c]).ravel() if obs.get(c) is not None else None) for c in "xyz"}
         check(lib().gb_misfit_set_obs(self._h, *[_ptr(arr[c]) for c in "xyz"]), "set_obs")
 
+    def set_obs_async(self, obs: dict):
+        """gb_misfit_set_obs_async: the copies overlap the next run's forward
+        pass; the arrays are kept alive here until that run returns."""
+        arr = {c: (_f32(obs[c]).ravel() if obs.get(c) is not None else None) for c in "xyz"}
+        check(lib().gb_misfit_set_obs_async(self._h, *[_ptr(arr[c]) for c in "xyz"]), "set_obs_async")
+        self._obs_hold = arr
+
     def run(self, kernel: bool = False, snapshot: bool = False) -> float:
         v = ctypes.c_double()
         check(lib().gb_misfit_run(self._h, int(kernel), int(snapshot), ctypes.byref(v)), "misfit run")
+        self._obs_hold = None
         return v.value
 
     def trace_values(self) -> np.ndarray:

@@ -207,6 +207,11 @@ struct gb_misfit {
     std::vector<cudaEvent_t> ev_r0, ev_r1;
     double *h_pin = nullptr;
     size_t h_pin_n = 0;
+    // observed traces queued by gb_misfit_set_obs_async: the upload stream,
+    // the event behind its copies, and whether the next run must wait for it
+    cudaStream_t st_up = nullptr;
+    cudaEvent_t ev_obs = nullptr;
+    bool obs_pending = false;
 
     int comps(int *c) const {
         int n = 0;
@@ -342,6 +347,7 @@ static int misfit_batch(gb_misfit *m, const int *shots, int n) {
     const int nc = m->comps(cs);
     const int ntr = n * nc * s.nrec;
     if (ntr == 0) return GB_OK;
+    if (m->obs_pending) GB_CUDA_TRY(cudaStreamWaitEvent(s.st, m->ev_obs, 0));
     GB_CUDA_TRY(cudaEventRecord(m->e0, s.st));
     if (m->type == 0) {
         k_waveform<<<ntr, 256, 0, s.st>>>(m->d_tr, m->tw, s.nt, std::sqrt(s.dt), m->d_val);
@@ -398,6 +404,7 @@ static int misfit_batch_pipe(gb_misfit *m, const int *shots, int n) {
         m->ev_r1.push_back(b);
     }
     cudaStream_t side = s.st_side;
+    if (m->obs_pending) GB_CUDA_TRY(cudaStreamWaitEvent(side, m->ev_obs, 0));
     for (int r = 0; r < s.pipe_rounds; r++) {
         const int b0 = r * s.pipe_occ, nb = std::min(s.pipe_occ, n - b0);
         const int tr0 = b0 * per_shot, ntr_r = nb * per_shot;
@@ -609,6 +616,10 @@ int gb_misfit_set_obs(gb_misfit *m, const float *ox, const float *oy, const floa
     Solver &s = *m->s;
     const float *h[3] = {ox, oy, oz};
     const size_t bytes = (size_t)s.nsrc * s.nrec * s.nt * 4;
+    if (m->obs_pending) {  // queued copies of gb_misfit_set_obs_async land first
+        GB_CUDA_TRY(cudaEventSynchronize(m->ev_obs));
+        m->obs_pending = false;
+    }
     for (int c = 0; c < 3; c++) {
         if (!m->obs[c]) continue;
         if (!h[c]) {
@@ -621,9 +632,39 @@ int gb_misfit_set_obs(gb_misfit *m, const float *ox, const float *oy, const floa
     return GB_OK;
 }
 
+int gb_misfit_set_obs_async(gb_misfit *m, const float *ox, const float *oy, const float *oz) {
+    if (!m) return GB_ERR_ARG;
+    Solver &s = *m->s;
+    const float *h[3] = {ox, oy, oz};
+    for (int c = 0; c < 3; c++)
+        if (m->obs[c] && !h[c]) {
+            set_error("gb_misfit_set_obs_async: component " + std::to_string(c) + " is used but was not given");
+            return GB_ERR_ARG;
+        }
+    if (!m->st_up) {
+        GB_CUDA_TRY(cudaStreamCreateWithFlags(&m->st_up, cudaStreamNonBlocking));
+        GB_CUDA_TRY(cudaEventCreateWithFlags(&m->ev_obs, cudaEventDisableTiming));
+    }
+    // (the solver's stream is idle between calls: no kernel of an earlier
+    // run still reads the observed traces)
+    const size_t bytes = (size_t)s.nsrc * s.nrec * s.nt * 4;
+    for (int c = 0; c < 3; c++)
+        if (m->obs[c]) GB_CUDA_TRY(cudaMemcpyAsync(m->obs[c], h[c], bytes, cudaMemcpyHostToDevice, m->st_up));
+    GB_CUDA_TRY(cudaEventRecord(m->ev_obs, m->st_up));
+    m->obs_pending = true;
+    return GB_OK;
+}
+
 int gb_misfit_run(gb_misfit *m, int kernel, int snapshot, double *value) {
     if (!m) return GB_ERR_ARG;
-    return misfit_run(m, kernel != 0, snapshot != 0, value);
+    const int rc = misfit_run(m, kernel != 0, snapshot != 0, value);
+    if (m->obs_pending) {
+        // the copies are complete once the run's misfit stages have run; an
+        // early error return waits for them here
+        GB_CUDA_TRY(cudaEventSynchronize(m->ev_obs));
+        m->obs_pending = false;
+    }
+    return rc;
 }
 
 int gb_misfit_trace_values(gb_misfit *m, double *out, size_t n) {
@@ -651,6 +692,8 @@ void gb_misfit_destroy(gb_misfit *m) {
     for (cudaEvent_t e : m->ev_r0) cudaEventDestroy(e);
     for (cudaEvent_t e : m->ev_r1) cudaEventDestroy(e);
     if (m->h_pin) cudaFreeHost(m->h_pin);
+    if (m->ev_obs) cudaEventDestroy(m->ev_obs);
+    if (m->st_up) cudaStreamDestroy(m->st_up);
     delete m;
 }
 

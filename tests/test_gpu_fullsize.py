@@ -160,3 +160,43 @@ def test_c2_pipelined_gradient_identical(gpu, orc, kind, wave):
     assert out[0][0] == out[1][0]
     for n in names:
         np.testing.assert_array_equal(out[0][1][n], out[1][1][n])
+
+
+@pytest.mark.parametrize("wave", ["sh", "psv"])
+def test_observed_traces_queued_during_the_forward_identical(gpu, orc, wave):
+    """gb_misfit_set_obs_async queues the observed traces' upload on a stream
+    of its own, overlapping the next run's forward pass (only the misfit
+    stages wait for it): on the C2 shapes (pipelined rounds) the misfit and
+    kernels are bit-identical to those of a run after gb_misfit_set_obs, and
+    the same holds on a grid that runs the per-step kernels."""
+    h = 12.5
+    for nx, nz, cluster in ((681, 141, 1), (200, 120, 0)):
+        case = surface_receivers(cases.make_case(wave=wave, nx=nx, nz=nz, nt=200, nsrc=16, dx=h, dt=1e-3, f0=8.0,
+                                                 abs_width=20, sfe=10, seed=3), h)
+        comps = "y" if wave == "sh" else "xz"
+        pert = dict(case)
+        pert["vs"] = (case["vs"] * 1.02).astype(np.float32)
+        cfg, sol = cases.gpu_solver(gpu, pert)
+        sol.set_option("batch", 16)
+        sol.run_forward_batch(list(range(16)))
+        obs = {c: np.stack([sol.out(c, slot=b) for b in range(16)]) for c in comps}
+        sol.close()
+        zeros = {c: np.zeros_like(v) for c, v in obs.items()}
+        out = []
+        for queued in (0, 1):
+            cfg, sol = cases.gpu_solver(gpu, case)
+            sol.set_option("batch", 16)
+            sol.set_option("cluster", cluster)
+            m = gpu.Misfit.from_obs(1, sol, zeros)
+            if queued:
+                m.set_obs_async(obs)
+            else:
+                m.set_obs(obs)
+            val = m.run(kernel=True)
+            out.append((val, sol.kernels()))
+            if cluster:
+                assert sol.stats().tile_tz < 0, "the cluster path did not run"
+            sol.close()
+        assert out[0][0] == out[1][0] and out[0][0] > 0
+        for n in out[0][1]:
+            np.testing.assert_array_equal(out[0][1][n], out[1][1][n])
