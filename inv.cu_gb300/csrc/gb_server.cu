@@ -7,12 +7,14 @@
 // it admits the requests that have arrived, in arrival order, while their
 // device footprint (model, wavefields, traces, checkpoints, kernels) fits the
 // HBM budget and a slot is free. A round advances every admitted request by
-// `sfe` steps: one step launch per wave system covers all of them, whatever
-// their grid size or phase (forward or adjoint), because every request keeps
-// its own time base in its slot descriptor. Requests that finish their
-// forward get their misfit and adjoint sources and start the adjoint in the
-// next round; requests that finish their adjoint return their kernels and
-// leave, freeing memory for waiting requests.
+// `sfe` steps: each wave system's requests form one or two groups, and one
+// step launch per group covers all of its requests, whatever their grid size
+// or phase (forward or adjoint), because every request keeps its own time
+// base in its slot descriptor; the groups' launch chains run on streams of
+// their own. Requests that finish their forward get their misfit and
+// adjoint sources and start the adjoint in the next round; requests that
+// finish their adjoint return their kernels and leave, freeing memory for
+// waiting requests. The host never waits for the GPU inside a run.
 //
 // Every request computes exactly the operations of a lone solve, in the
 // same order, so its result does not depend on what else is in flight.
