@@ -527,6 +527,13 @@ int Solver::ensure_slots(int n) {
                       " bytes, more than the HBM budget");
             return GB_ERR_BUDGET;
         }
+        // equal batches: as many as the budget needs, as even as possible
+        // (64 shots at a budget of 60 run as 32 + 32, not 60 + 4, whose small
+        // batch fills the GPU poorly)
+        if (cap < nsrc) {
+            const long nb = (nsrc + cap - 1) / cap;
+            cap = (nsrc + nb - 1) / nb;
+        }
         capacity = (int)cap;
         for (int q = 0; q < 3; q++) {
             GB_CUDA_TRY(cudaMalloc(&d_slots[q], sizeof(Slot) * capacity));

@@ -133,3 +133,37 @@ def test_served_request_with_odd_nz_matches_oracle(gpu, orc):
     kern = orc.adjoint(pb, [ad["x"], ad["y"], ad["z"]], o[3])
     for q, name in enumerate(("k_lambda", "k_mu", "k_rho")):
         assert cases.rel(res[name], kern[q]) < 1e-4, name
+
+
+def test_many_completions_share_the_pinned_result_buffers(gpu):
+    """Finished requests' kernels are copied out through a pool of eight
+    pinned buffers and finalised when their copies complete; with twenty
+    requests of different lengths in flight, completions outnumber the
+    buffers and some wait for a buffer to be finalised. Every result is
+    bit-identical to the same request served one at a time, and latencies
+    (completion time from the copies' event) are ordered with the requests'
+    lengths at equal arrival."""
+    mix = [(q % 2, 48 + 8 * (q % 5), 40 + 4 * (q % 3), 100 + 20 * (q % 4), 40 + q) for q in range(20)]
+    reqs = [request(*m, nrec=8)[1] for m in mix]
+    srv = gpu.Server(sfe=10)
+    ids = [srv.submit(arrival=0.0, **r) for r in reqs]
+    srv.run()
+    st = srv.stats()
+    assert st.completed == len(reqs) and st.max_concurrent == len(reqs)
+    together = [srv.result(i) for i in ids]
+    one = gpu.Server(sfe=10, max_slots=1)
+    ids1 = [one.submit(arrival=0.0, **r) for r in reqs]
+    one.run()
+    for q, i in enumerate(ids1):
+        res = one.result(i)
+        for name in ("k_lambda", "k_mu", "k_rho"):
+            np.testing.assert_array_equal(res[name], together[q][name])
+        assert res["misfit"] == together[q]["misfit"]
+    # all admitted at t = 0 and advanced in lockstep: a request with fewer
+    # steps never finishes after one with more
+    lat = [r["latency"] for r in together]
+    nts = [r["nt"] for r in reqs]
+    for a in range(len(reqs)):
+        for b in range(len(reqs)):
+            if nts[a] < nts[b]:
+                assert lat[a] <= lat[b]
