@@ -119,9 +119,9 @@ struct Server {
     int tab_cap = 0;
     // Block maps of the round's marching launches (option "compact", on by
     // default): one entry per tile of every request, (slot << 16) | tile,
-    // P-SV entries first, staged like the tables. Without them a launch runs
-    // max_tiles blocks for every request and the blocks past a smaller
-    // request's tiles exit at once.
+    // one range per launch chain, staged like the tables. Without them a
+    // launch runs max_tiles blocks for every request and the blocks past a
+    // smaller request's tiles exit at once.
     bool compact = true;
     unsigned *d_map = nullptr, *h_map[kStage] = {};
     size_t map_cap = 0;
