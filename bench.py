@@ -549,6 +549,28 @@ def run_c1(args):
         mis.run(kernel=True)
         ms.append(sol.timer_end())
     grad_ms = sum(ms) / len(ms)
+    init_model = lame(init[1], init[0], init[2])
+    # the same gradient through the plain path (one shot per call, one fused
+    # step launch per time step, no CUDA graphs, no cluster pass)
+    plain = None
+    if not args.no_plain:
+        cfgp, sp = _solver_for(pkg, tmp, dict(values, batch=1, graphs=0, cluster=0), src, rec, nx, nz, h, init_model)
+        sp.set_option("batch", 1)
+        sp.set_option("graphs", 0)
+        sp.set_option("cluster", 0)
+        mp = pkg.Misfit.from_obs(0, sp, obs, pkg.GaussianFilter(nx, nz, 5))
+        mp.run(kernel=True)
+        sp.timer_begin()
+        mp.run(kernel=True)
+        plain_ms = sp.timer_end()
+        plain = {"value": round(4 / (plain_ms / 1e3), 2), "unit": "shots/s", "ms_per_step": round(plain_ms, 2)}
+        mp.close()
+        sp.close()
+    ref_gpu = None
+    if not args.no_ref_gpu:
+        ref_gpu = _c1_reference_gpu(values, src, rec, nx, nz, h, init_model, obs)
+        if "value" in ref_gpu:
+            ref_gpu["ours_over_reference"] = round((4 / (grad_ms / 1e3)) / ref_gpu["value"], 2)
     opt = pkg.Optimizer(cfg, sol, mis)
     t0 = time.perf_counter()
     opt.run()
@@ -558,8 +580,59 @@ def run_c1(args):
           {"workload": "P-SV 200x200 checkerboard +-5% in 20-cell squares, nt 2000, 4 shots, waveform misfit, "
                        "then 5 NLCG iterations", "receivers_depth_m": 2 * h},
           ms_per_step=round(grad_ms, 3), steps=args.steps, warmup=args.warmup,
+          plain_path=plain, reference_gpu=ref_gpu,
           inversion={"iterations": 5, "wall_s": round(inv_s, 3), "misfit_history": [round(v, 6) for v in hist],
                      "final_over_initial": round(hist[-1] / hist[0], 6) if len(hist) else None})
+
+
+def _c1_reference_gpu(values, src, rec, nx, nz, h, model, obs):
+    """One C1 gradient (4 P-SV shots, waveform misfit, smoothing of the
+    lambda and mu kernels) through the reference's own CUDA kernels in its
+    launch shapes and host loop (solver/fdm.h:515-612, misfit/waveform.h,
+    filter/gaussian.h), after one warm-up shot; wall time, no extrapolation."""
+    from oracle import oracle as orc
+
+    if not orc.ref_available():
+        return {"unavailable": "the reference's kernels were not built (oracle/_ref/inv_ref.cubin absent)"}
+    f32 = np.float32
+    nt, dt = values["nt"], values["dt"]
+    xmax = zmax = (nx - 1) * h
+    srca, reca = np.array(src, f32), np.array(rec, f32)
+    stf = [np.zeros(len(srca) * nt, f32) for _ in range(3)]
+    for s in range(len(srca)):
+        c = orc.ricker(nt, dt, *srca[s, 3:7])
+        for q in range(3):
+            stf[q][s * nt:(s + 1) * nt] = c[q]
+    ab = orc.absbound(nx, nz, values["abs_width"], values["abs_alpha"], values["abs_left"], values["abs_right"],
+                      values["abs_bottom"], values["abs_top"])
+    dx = float(f32(xmax) / f32(nx - 1))
+    lam, mu, rho = model
+    pb = orc.Problem(nx=nx, nz=nz, nt=nt, dx=dx, dz=dx, dt=float(f32(dt)), sh=False, psv=True, sfe=values["sfe"],
+                     lam=lam, mu=mu, rho=rho, ab=ab, stf=tuple(stf),
+                     src_id=(orc.calc_idx(srca[:, 0], float(xmax), nx), orc.calc_idx(srca[:, 1], float(zmax), nz)),
+                     rec_id=(orc.calc_idx(reca[:, 0], float(xmax), nx), orc.calc_idx(reca[:, 1], float(zmax), nz)),
+                     inv_lambda=True, inv_mu=True, inv_rho=False)
+    nrec = len(reca)
+
+    def shot(s, kern):
+        ox, _, oz, ck = orc.ref_forward(pb, s, adj=True)
+        _, adx = orc.ref_misfit(0, ox.reshape(nrec, nt), obs["x"][s], dt)
+        _, adz = orc.ref_misfit(0, oz.reshape(nrec, nt), obs["z"][s], dt)
+        return orc.ref_adjoint(pb, [adx, np.zeros_like(adx), adz], ck, kern)
+
+    shot(0, None)  # warm-up: module load, cuFFT/cuBLAS handles, first launches
+    t0 = time.perf_counter()
+    kern = None
+    for s in range(len(srca)):
+        kern = shot(s, kern)
+    for q in (0, 1):
+        orc.ref_gaussian(nx, nz, 5, kern[q])
+    t = time.perf_counter() - t0
+    return {"value": round(len(srca) / t, 3), "unit": "shots/s", "ms_per_gradient": round(1e3 * t, 1),
+            "sample": "one full 4-shot gradient, wall time (no extrapolation)",
+            "what": "the reference's own kernels compiled from its sources for sm_103a, run in its launch shapes "
+                    "and host loop: six launches per step, checkpoints to pageable host memory by blocking "
+                    "copies, per-trace waveform misfit with cuBLAS, its Gaussian filter"}
 
 
 def run_c3(args):
