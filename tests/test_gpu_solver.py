@@ -230,3 +230,20 @@ def test_both_wave_systems_in_one_solver(gpu, orc):
     o = orc.forward(pb, 0, adj=True)
     for c in "xyz":
         assert cases.rel(sol.out(c), o["xyz".index(c)]) < TRACE_TOL
+
+
+@pytest.mark.parametrize("wave", ["psv", "sh"])
+def test_adjoint_rejects_nt_not_a_multiple_of_sfe(gpu, wave):
+    """With nt % sfe != 0 the reference's adjoint pairs its steps with the
+    wrong checkpoints and reads slot nsfe, one past its array
+    (solver/fdm.h:391,583-584). The library's adjoint refuses such a
+    configuration with an error that says why, and the solver stays usable.
+    The forward pass runs, and its checkpoint slots stay inside the array."""
+    case = cases.make_case(wave=wave, nx=64, nz=48, nt=205, nsrc=1, nrec=8, sfe=10, seed=5)
+    cfg, sol = cases.gpu_solver(gpu, case)
+    sol.run_forward_batch([0])
+    assert np.isfinite(sol.out(comps(wave)[0])).all()
+    sol.initKernels()
+    with pytest.raises(gpu.GbError, match="multiple of sfe"):
+        sol.run_adjoint_batch([0])
+    sol.run_forward_batch([0])  # still usable
